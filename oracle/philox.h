@@ -1,0 +1,28 @@
+/*
+ * philox.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11) for the CPU checkers.  Each round multiplies
+ * counter words 0 and 2 by the two Philox multipliers (32x32 -> 64 bits) and
+ * emits (hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0); the key is bumped by the two
+ * Weyl constants between rounds.
+ */
+#ifndef TRW_ORACLE_PHILOX_H
+#define TRW_ORACLE_PHILOX_H
+
+#include <stdint.h>
+
+static inline void oracle_philox_block(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+    }
+}
+
+#endif
