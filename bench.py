@@ -1,0 +1,444 @@
+#!/usr/bin/env python
+"""Walk-steps/s benchmark of the GB300 random-walk engine.
+
+Default workload (the batched-PPR configuration): R-MAT graph (a,b,c =
+0.57,0.19,0.19), N = 2^22 vertices, average degree 32 before symmetrisation,
+undirected int32 CSR; 4096 queries x 10^4 walkers whose sources are drawn
+uniformly among non-isolated vertices; uniform sampling, termination
+probability 0.2 after every move (geometric lengths, mean 5); output: int32
+visit counts per query (4096 x N, zeroed inside every step).  One step = one
+whole batch through trw_ppr_batch.  Inputs (adjacency 0.5 GB, counts 64 GiB)
+are far larger than the 129 MB L2, so no separate flush is needed.
+
+Prints one JSON line (rank 0).  --impl reference times the reference's CPU
+algorithm (the step-interleaved C++ oracle port of creeper.h's ring) on the
+host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+BYTES_PER_STEP = {
+    # Algorithmic bytes per move (32-byte sectors of each independent random
+    # access, 4 bytes per path entry): row pair 32 + adjacency entry 32 +
+    # visit-count update 32.
+    "ppr": 96,
+    # row pair 32 + alias slot 32 + path entry 4
+    "deepwalk": 68,
+}
+
+WORKLOADS = {
+    "ppr": dict(kind="rmat", n=1 << 22, deg=32, queries=4096, per_query=10_000, tp=0.2,
+                name="ppr_batch rmat(0.57,0.19,0.19) N=2^22 deg=32 undirected, 4096 queries x 1e4 walkers, "
+                     "uniform sampling tp=0.2, int32 visit counts per query"),
+    "deepwalk": dict(kind="chunglu", n=1 << 18, deg=16, length=80,
+                     name="deepwalk static alias chung-lu(2.1) N=2^18 deg=16, one walker per vertex, L=80"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ppr", choices=sorted(WORKLOADS))
+    ap.add_argument("--queries", type=int, default=None, help="override the query count (small runs)")
+    ap.add_argument("--scale", type=int, default=None, help="override log2(N) (small runs)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload construction
+# ---------------------------------------------------------------------------
+
+def build_inputs(wl, args, device):
+    import torch
+    from thunderrw_gb300 import generators as G
+    n = 1 << args.scale if args.scale else wl["n"]
+    g = G.make_graph(wl["kind"], n, wl["deg"], seed=20240601, device=device, weights=wl["kind"] != "rmat",
+                     labels=0)
+    out = {"n": n, "row": g["row"], "adj": g["adj"], "weight": g["weight"]}
+    if "queries" in wl:
+        q = args.queries or wl["queries"]
+        out["sources"] = G.random_sources(g["row"], q, seed=7)
+        out["per_query"] = wl["per_query"]
+    else:
+        out["sources"] = G.all_sources(g["row"], seed=0)
+    torch.cuda.synchronize()
+    return out
+
+
+def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, threads):
+    """The step-interleaved CPU port (oracle) on a bounded sample of the same
+    workload, on all host threads.  Returns (steps/s, sample description)."""
+    from oracle import oracle as O
+    og = O.Graph(row, adj, weight)
+    ncores = threads or os.cpu_count()
+    if wl_name == "ppr":
+        d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=wl["tp"], seed=11)
+        chunk = 16  # queries per pass; each pass zeroes and fills a 16 x N count block
+        counts = np.zeros((chunk, og.n), dtype=np.int32)
+        total_steps, total_t, done_q = 0, 0.0, 0
+        src = np.asarray(sources, dtype=np.int32)
+        while total_t < seconds and done_q < src.size:
+            qs = src[done_q:done_q + chunk]
+            t0 = time.perf_counter()
+            counts[: qs.size].fill(0)
+            r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_counts=True,
+                       want_lengths=False, num_queries=chunk, threads=ncores, interleaved=True, ring=64)
+            total_t += time.perf_counter() - t0
+            total_steps += r["steps"]
+            done_q += qs.size
+        sample = "%d queries x %d walkers (%d steps) in %.1f s" % (done_q, per_query, total_steps, total_t)
+        return total_steps / total_t, sample, ncores
+    og.build_tables("alias", 0)
+    d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=11)
+    src = np.asarray(sources, dtype=np.int32)
+    total_steps, total_t, done = 0, 0.0, 0
+    chunk = 1 << 16
+    paths = None
+    while total_t < seconds and done < src.size:
+        s = src[done:done + chunk]
+        t0 = time.perf_counter()
+        r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=True, ring=64)
+        total_t += time.perf_counter() - t0
+        total_steps += r["steps"]
+        done += s.size
+        paths = r["paths"]
+    del paths
+    return total_steps / total_t, "%d walkers x %d steps (%d steps) in %.1f s" % (
+        done, wl["length"] - 1, total_steps, total_t), ncores
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    wl = WORKLOADS[args.workload]
+    have_gpu = torch.cuda.is_available()
+    inp = build_inputs(wl, args, "cuda" if have_gpu else "cpu")
+    row = inp["row"].cpu().numpy()
+    adj = inp["adj"].cpu().numpy()
+    weight = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
+    src = inp["sources"].cpu().numpy()
+    per_q = inp.get("per_query", 0)
+    del inp
+    if have_gpu:
+        torch.cuda.empty_cache()
+    vals = []
+    sample = ""
+    cores = os.cpu_count()
+    for i in range(args.warmup + args.steps):
+        v, sample, cores = cpu_baseline(args.workload, wl, row, adj, weight, src, per_q,
+                                        max(2.0, 20.0 / max(1, args.warmup + args.steps)), 0)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "walk_steps_per_s", "value": value, "unit": "steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
+        "config": {"workload": wl["name"]},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
+                         "sample": "step-interleaved C++ port of the reference ring (64 walkers per thread), "
+                                   "per step " + sample},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import engine as E
+
+    wl = WORKLOADS[args.workload]
+    inp = build_inputs(wl, args, dev)
+    graph = E.Graph(inp["row"], inp["adj"], inp["weight"])
+    stream = torch.cuda.current_stream(dev)
+    L = N.load()
+    import ctypes
+
+    if args.workload == "ppr":
+        Q = inp["sources"].numel()
+        per_q = inp["per_query"]
+        counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
+        steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
+        src = inp["sources"]
+
+        def one_step(seed, engine="persistent", zero=True):
+            d = E.PPR(wl["tp"]).desc(seed)
+            N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q, per_q,
+                                    ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(steps_dev.data_ptr()),
+                                    1 if zero else 0, N.ENGINES[engine], ctypes.c_void_p(stream.cuda_stream)))
+    else:
+        src = inp["sources"]
+        W = src.numel()
+        Lw = wl["length"]
+        paths = torch.empty((W, Lw), dtype=torch.int32, device=dev)
+        lengths = torch.empty(W, dtype=torch.int32, device=dev)
+        steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
+        counts = None
+        graph.build_tables("alias", "edge")
+
+        def one_step(seed, engine="persistent", zero=True):
+            d = E.DeepWalk(Lw).desc(seed)
+            N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), W, 0,
+                               ctypes.c_void_p(paths.data_ptr()), Lw, ctypes.c_void_p(lengths.data_ptr()), None,
+                               ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
+                               ctypes.c_void_p(stream.cuda_stream)))
+
+    # ---- warm-up
+    for i in range(args.warmup):
+        one_step(1000 + i)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K whole batches, fresh seeds
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    total_steps = 0
+    ev0.record(stream)
+    for i in range(args.steps):
+        one_step(2000 + i)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_total = ev0.elapsed_time(ev1) / 1e3
+    # per-launch walk-kernel time (the counts are zeroed before the kernel
+    # starts; these events bracket the walk launch alone)
+    kern_ms = []
+    for i in range(args.steps):
+        if counts is not None:
+            counts.zero_()
+        a, b = step_evs[i]
+        a.record(stream)
+        one_step(2000 + i, zero=False)
+        b.record(stream)
+        torch.cuda.synchronize()
+        kern_ms.append(a.elapsed_time(b))
+        total_steps += int(steps_dev.item())
+    clocks = sampler.stop()
+    steps_per_batch = total_steps / args.steps
+    if world > 1:
+        t = torch.tensor([t_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+        s = torch.tensor([steps_per_batch * args.steps], device=dev, dtype=torch.float64)
+        dist.all_reduce(s)
+        all_steps = float(s.item())
+    else:
+        all_steps = steps_per_batch * args.steps
+    value = all_steps / t_total
+
+    # ---- e2e: through the C ABI with host buffers (pinned sources in, steps out)
+    h_src = src.cpu().pin_memory()
+    h_steps = torch.zeros(1, dtype=torch.int64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = 0
+    for i in range(args.steps):
+        if args.workload == "ppr":
+            d = E.PPR(wl["tp"]).desc(3000 + i)
+            N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
+                                    ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(h_steps.data_ptr()), 1, 0,
+                                    ctypes.c_void_p(stream.cuda_stream)))
+        else:
+            d = E.DeepWalk(wl["length"]).desc(3000 + i)
+            N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
+                               ctypes.c_void_p(paths.data_ptr()), wl["length"], ctypes.c_void_p(lengths.data_ptr()),
+                               None, ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
+        e2e_steps += int(h_steps.item())
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    e2e = {"value": e2e_steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": int(h_src.numel() * 4),
+           "d2h_bytes_per_step": 8}
+
+    # ---- plain one-launch-per-query form (the comparison engine)
+    plain = None
+    if not args.no_plain:
+        reps = max(1, min(3, args.steps))
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if args.workload == "ppr":
+            a.record(stream)
+            for r in range(reps):
+                counts.zero_()
+                for qi in range(Q):
+                    d = E.PPR(wl["tp"]).desc(4000 + r)
+                    N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr() + 4 * qi), 1,
+                                            per_q, ctypes.c_void_p(counts.data_ptr() + 4 * qi * graph.n),
+                                            ctypes.c_void_p(steps_dev.data_ptr()), 0, 1,
+                                            ctypes.c_void_p(stream.cuda_stream)))
+            b.record(stream)
+            torch.cuda.synchronize()
+        else:
+            a.record(stream)
+            for r in range(reps):
+                one_step(4000 + r, engine="plain")
+            b.record(stream)
+            torch.cuda.synchronize()
+        plain_t = a.elapsed_time(b) / 1e3 / reps
+        plain = {"value": steps_per_batch / plain_t, "unit": "steps/s", "ms_per_step": plain_t * 1e3,
+                 "form": "one thread per walker, one launch per query, no refill"}
+
+    # ---- roofline of the walk kernel
+    kmean = statistics.mean(kern_ms) / 1e3
+    bps = BYTES_PER_STEP[args.workload]
+    achieved = steps_per_batch * bps / kmean / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_per_step.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tv = json.load(f).get(args.workload)
+        if tv:
+            traffic = tv * steps_per_batch
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "bytes_per_step": bps, "kernel_ms": kmean * 1e3,
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        row = inp["row"].cpu().numpy()
+        adj = inp["adj"].cpu().numpy()
+        wt = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
+        v, sample, cores = cpu_baseline(args.workload, wl, row, adj, wt, src.cpu().numpy(),
+                                        inp.get("per_query", 0), args.cpu_seconds, 0)
+        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
+               "sample": "step-interleaved C++ port of the reference ring, " + sample}
+
+    if rank == 0:
+        line = {
+            "metric": "walk_steps_per_s", "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": wl["name"], "n": graph.n, "e": graph.e,
+                       "steps_per_batch": steps_per_batch, "engine": "persistent",
+                       "l2": "inputs larger than L2 (adjacency %.2f GB, counts %.1f GB)" % (
+                           graph.e * 4 / 1e9, (counts.numel() * 4 / 1e9) if counts is not None else 0)},
+            "gpu_launches": args.steps, "clocks": clocks, "e2e": e2e, "roofline": roof,
+            "plain": plain, "vs_plain": (value / plain["value"]) if plain else None, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    graph.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

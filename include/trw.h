@@ -1,0 +1,193 @@
+/*
+ * trw.h -- C ABI of libtrw_gpu.so, the GB300 random-walk engine.
+ *
+ * Drop-in boundary for ThunderRW's walk path (Gather-Move-Update,
+ * random_walk/creeper.h).  The reference exposes header-only C++ templates
+ * (compute<F>(Graph&, std::vector<WalkerMeta>&, F), creeper.h:689) with
+ * per-app functors and process globals (g_para, types.h:109); this ABI carries
+ * the same information as plain values and pointers so any host language can
+ * bind it.  Every function returns TRW_OK (0) or a negative trw_status and
+ * never aborts the process; trw_last_error() describes the last failure on
+ * the calling thread.
+ *
+ * Pointers passed for walk inputs and outputs may be host or device memory:
+ * the library inspects each pointer, stages host buffers through HBM and
+ * copies host outputs back before returning (such calls synchronise the
+ * stream).  With device pointers the call only enqueues work on `stream`.
+ *
+ * Randomness: every walker draws from Philox4x32-10 with
+ *   key = (seed lo, seed hi), counter = (block, step, walker lo, walker hi),
+ * where step is the walker's length before the move (1 for the first move),
+ * draw d of one move uses block d/4 and word d%4, and the PPR termination
+ * draw uses block TRW_TERM_BLOCK with step = length after the move.  Results
+ * therefore do not depend on scheduling, engine choice or batching.
+ */
+#ifndef TRW_H
+#define TRW_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct trw_graph trw_graph;
+typedef struct CUstream_st *trw_stream_t; /* a cudaStream_t; NULL = legacy default stream */
+
+#define TRW_TERM_BLOCK 0x80000000u
+
+enum trw_status {
+    TRW_OK = 0,
+    TRW_ERR_INVALID = -1,      /* bad argument */
+    TRW_ERR_CUDA = -2,         /* CUDA runtime error (message in trw_last_error) */
+    TRW_ERR_UNSUPPORTED = -3,  /* app / mode / sampler combination not supported */
+    TRW_ERR_NO_TABLES = -4,    /* static sampler used before trw_tables_build */
+    TRW_ERR_GRAPH = -5,        /* graph failed validation */
+    TRW_ERR_DEVICE = -6,       /* a kernel raised its device error word */
+    TRW_ERR_CAPACITY = -7,     /* size above a stated maximum */
+    TRW_ERR_BUSY = -8          /* serving queue full */
+};
+
+/* App hooks (random_walk/apps/*.cpp).  DeepWalk and GenericWalk share hooks:
+ * weight = edge weight, update = (length == l), max_weight = 5.0. */
+enum trw_app {
+    TRW_APP_DEEPWALK = 0,   /* deepwalk.cpp:9-30 */
+    TRW_APP_PPR = 1,        /* ppr.cpp:10-34: weight 1, update real1 <= tp */
+    TRW_APP_NODE2VEC = 2,   /* node2vec.cpp:9-47: weight {1/p, 1, 1/q} */
+    TRW_APP_METAPATH = 3,   /* metapath.cpp:9-39: weight [label == schema[(len-1)%S]] */
+    TRW_APP_GENERICWALK = 4 /* genericwalk.cpp:9-30 */
+};
+
+/* ExecutionMode (types.h:41-45) and SamplingMethod (types.h:53-59). */
+enum trw_mode { TRW_MODE_UNIFORM = 0, TRW_MODE_STATIC = 1, TRW_MODE_DYNAMIC = 2 };
+enum trw_sampler {
+    TRW_SAMPLER_UNIFORM = 0,
+    TRW_SAMPLER_ITS = 1,
+    TRW_SAMPLER_ALIAS = 2,
+    TRW_SAMPLER_REJECTION = 3,
+    TRW_SAMPLER_MAXWEIGHT_REJECTION = 4
+};
+
+/* Static-table weights: what static_gather (creeper.h:24-99) produces for
+ * the app: edge weights (DeepWalk, GenericWalk) or 1.0 (PPR). */
+enum trw_weight_kind { TRW_WEIGHTS_EDGE = 0, TRW_WEIGHTS_UNIT = 1 };
+
+/* Engine: the persistent batched engine (warps keep several walkers in
+ * flight and refill them from a device work queue) or the plain form (one
+ * thread per walker, one launch per call, no refill). */
+enum trw_engine { TRW_ENGINE_PERSISTENT = 0, TRW_ENGINE_PLAIN = 1 };
+
+/* AliasSlot (config/type_config.h:22-26), byte-identical layout. */
+typedef struct {
+    double prob;
+    int32_t first;
+    int32_t second;
+} trw_alias_slot;
+
+#define TRW_MAX_SCHEMA 64
+
+/* The per-run parameters the reference takes from g_para (types.h:72-77,109)
+ * and from the app functor's constructor arguments. */
+typedef struct {
+    int32_t app;          /* trw_app */
+    int32_t mode;         /* trw_mode (g_para.execution_) */
+    int32_t sampler;      /* trw_sampler (g_para.sample_) */
+    int32_t length;       /* l_: walk length of the fixed-length apps */
+    double p;             /* Node2Vec return parameter; return edges weigh 1/p */
+    double q;             /* Node2Vec in-out parameter; other edges weigh 1/q */
+    double tp;            /* PPR termination probability */
+    const int32_t *schema;/* MetaPath schema (host memory), <= TRW_MAX_SCHEMA */
+    int32_t schema_len;
+    uint64_t seed;        /* Philox key */
+} trw_walk_desc;
+
+/* ---- graph ------------------------------------------------------------ */
+
+#define TRW_GRAPH_CHECK_SORTED 1u  /* also verify sorted neighbour lists (graph.cpp:764-776) */
+
+/* Replaces Graph::load_csr's in-memory result (util/graph/graph.cpp:45-101;
+ * CSR arrays graph.h:51-65, offset_pair_ graph.cpp:86-91).  Copies the CSR
+ * (row_ptr n+1 int64, adj e int32, optional weight e double, optional label
+ * e int32) into library-owned HBM; the caller keeps its arrays.  Validates
+ * row_ptr monotonicity, adjacency range and e < 2^31. */
+int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *weight,
+                     const int32_t *label, int32_t n, int64_t e, uint32_t flags,
+                     trw_graph **out);
+
+/* Replaces Graph::~Graph (graph.h:118-145). */
+int trw_graph_destroy(trw_graph *g);
+
+/* num_vertices / num_edges / max_degree (graph.h:152-166). */
+int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degree);
+
+/* ---- static tables ---------------------------------------------------- */
+
+/* Replaces static_initialization (creeper.h:102-175) and the offline
+ * builders alias_preprocess.cpp:30-73, its_preprocess.cpp:21-34 and
+ * rejection_preprocess.cpp:24-27: builds the alias table, the ITS prefix
+ * sums or the rejection per-vertex maxima in HBM with device kernels,
+ * bit-identical to the reference's sequential double arithmetic. */
+int trw_tables_build(trw_graph *g, int32_t sampler, int32_t weight_kind, trw_stream_t stream);
+
+/* Copies a built table to `out` (host or device): alias -> e trw_alias_slot
+ * (edge_weight_alias_table_, graph.h:77), ITS -> e doubles
+ * (edge_weight_prefix_sum_, graph.h:70), rejection -> n doubles
+ * (edge_weight_rejection_max_, graph.h:83). */
+int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t out_bytes);
+
+/* ---- walks ------------------------------------------------------------ */
+
+/* Replaces compute<F>(graph, walkers, f) (creeper.h:689-831) for the five
+ * reference apps, every mode x sampler pair of types.h:41-59.
+ *   sources[i]      start vertex of walker i (WalkerMeta::source_, walker.h:9-15)
+ *   id_base         Philox walker id of walker 0 (walker i uses id_base + i)
+ *   paths           num_walkers x path_cap int32, walker-major, or NULL; entry
+ *                   k < length holds the k-th vertex of the walk (seq_[k],
+ *                   creeper.h:310-317), later entries are -1
+ *   lengths         num_walkers int32 final length_ values, or NULL
+ *   counts          n int32 visit counters, or NULL: every move adds 1 to
+ *                   counts[new vertex] (so sum(counts) = steps); counts are
+ *                   added to, not overwritten
+ *   steps           receives the number of moves (creeper.h:305), or NULL
+ * Walkers at a vertex without neighbours stop (the reference divides by zero
+ * there). */
+int trw_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_walkers,
+             int64_t id_base, int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts,
+             uint64_t *steps, int32_t engine, trw_stream_t stream);
+
+/* Batched PPR: num_queries queries of walkers_per_query walkers each, all
+ * in one launch.  Walker j of query q starts at sources[q] and has Philox id
+ * q * walkers_per_query + j.  counts is num_queries x n int32 (query-major);
+ * each move adds 1 to counts[q][new vertex].  With TRW_PPR_ZERO_COUNTS the
+ * library zeroes counts first; otherwise counts are added to.  The reference
+ * runs PPR as one compute() per source with no visit counter (ppr.cpp:37-84,
+ * walker_generator.cpp:42-63); this entry point replaces a loop of those. */
+#define TRW_PPR_ZERO_COUNTS 1u
+int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
+                  int64_t walkers_per_query, int32_t *counts, uint64_t *steps, uint32_t flags,
+                  int32_t engine, trw_stream_t stream);
+
+/* Autotuned launch shape of the persistent engine for this graph and
+ * sampler: walkers per thread (ring depth) and CTAs per SM.  0 = default. */
+int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm);
+int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_per_thread,
+                         int32_t *ctas_per_sm);
+
+/* ---- errors ----------------------------------------------------------- */
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *trw_last_error(void);
+
+/* Reads and clears the graph's device error word (1 = a rejection sampler
+ * exceeded its trial limit, 2 = invalid vertex met in a walk). */
+int trw_device_error(trw_graph *g, int32_t *code);
+
+/* Library version, e.g. 1000 for 1.0.0. */
+int32_t trw_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRW_H */

@@ -336,7 +336,7 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
         w.len += 1;
         /* update (creeper.h:299-319) */
         steps += 1;
-        if (counts) { counts[nxt] += 1; if (kCount) bc->bytes += 32; }
+        if (counts) { __atomic_fetch_add(counts + nxt, 1, __ATOMIC_RELAXED); if (kCount) bc->bytes += 32; }
         if (app.update(d->seed, wid, w)) break;
     }
     if (path) for (int32_t k = w.len; k < path_cap; ++k) path[k] = -1;
@@ -346,6 +346,11 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
 int validate(const oracle_graph *g, const oracle_walk_desc *d) {
     if (!g || !d || !g->row || !g->adj) return -1;
     if (d->mode < 0 || d->mode > 2 || d->sampler < 0 || d->sampler > 4 || d->app < 0 || d->app > 4) return -2;
+    /* the walks that would never end in the reference: l_ < 2, tp <= 0 */
+    if (d->app != APP_PPR && d->length < 2) return -1;
+    if (d->app == APP_PPR && !(d->tp >= 1e-6 && d->tp <= 1.0)) return -1;
+    if (d->app == APP_NODE2VEC && !(d->p > 0.0 && d->q > 0.0)) return -1;
+    if (d->app == APP_METAPATH && d->mode == MODE_DYNAMIC && d->sampler == S_MAXRS) return -3;
     if (d->mode == MODE_STATIC) {
         if (d->app == APP_NODE2VEC || d->app == APP_METAPATH) return -3;
         if (d->sampler == S_ALIAS && !g->alias) return -4;
@@ -456,17 +461,13 @@ int oracle_walk(const oracle_graph *g, const oracle_walk_desc *d, const int32_t 
     const App app(d);
     int32_t nt = nthreads(threads);
     std::vector<uint64_t> tsteps(nt, 0);
-    /* visit counts are summed per thread to keep the threads independent */
-    std::vector<std::vector<int32_t>> tcounts;
-    int64_t nq = per_query > 0 ? (num_walkers + per_query - 1) / per_query : 1;
-    if (counts) tcounts.resize(nt);
+    /* visit counts are added with relaxed atomics straight into `counts` */
     parallel_for(num_walkers, nt, [&](int tid, int64_t b, int64_t e) {
         Scratch sc;
-        if (counts && tcounts[tid].empty()) tcounts[tid].assign((size_t)nq * g->n, 0);
         for (int64_t i = b; i < e; ++i) {
             int64_t qi = per_query > 0 ? i / per_query : 0;
             int32_t src = per_query > 0 ? sources[qi] : sources[i];
-            int32_t *crow = counts ? tcounts[tid].data() + (size_t)qi * g->n : nullptr;
+            int32_t *crow = counts ? counts + (size_t)qi * g->n : nullptr;
             walk_one<false>(g, d, app, (uint64_t)(id_base + i), src,
                             paths ? paths + (size_t)i * path_cap : nullptr, path_cap,
                             lengths ? lengths + i : nullptr, crow, tsteps[tid], sc, nullptr);
@@ -475,12 +476,6 @@ int oracle_walk(const oracle_graph *g, const oracle_walk_desc *d, const int32_t 
     uint64_t total = 0;
     for (uint64_t s : tsteps) total += s;
     if (steps) *steps = total;
-    if (counts) {
-        for (auto &tc : tcounts) {
-            if (tc.empty()) continue;
-            for (size_t k = 0; k < tc.size(); ++k) counts[k] += tc[k];
-        }
-    }
     return 0;
 }
 
@@ -533,13 +528,10 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
     const App app(d);
     const int32_t nt = nthreads(threads);
     std::vector<uint64_t> tsteps(nt, 0);
-    int64_t nq = per_query > 0 ? (num_walkers + per_query - 1) / per_query : 1;
-    std::vector<std::vector<int32_t>> tcounts(counts ? nt : 0);
     /* static walker chunks per thread, as creeper.h:729-734 */
     auto body = [&](int tid) {
         int64_t chunk = num_walkers / nt;
         int64_t b = tid * chunk, e = tid == nt - 1 ? num_walkers : b + chunk;
-        if (counts) tcounts[tid].assign((size_t)nq * g->n, 0);
         struct Slot { bool empty; int64_t idx; Walker w; int64_t pos; int64_t off; int32_t deg; uint32_t u0, u1; };
         std::vector<Slot> r(ring);
         int64_t next = b;
@@ -591,7 +583,7 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
                     st += 1;
                     if (counts) {
                         int64_t qi = per_query > 0 ? s.idx / per_query : 0;
-                        tcounts[tid][(size_t)qi * g->n + nxt] += 1;
+                        __atomic_fetch_add(counts + (size_t)qi * g->n + nxt, 1, __ATOMIC_RELAXED);
                     }
                     done = app.update(d->seed, (uint64_t)(id_base + s.idx), s.w);
                 }
@@ -609,7 +601,6 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
     uint64_t total = 0;
     for (uint64_t s : tsteps) total += s;
     if (steps) *steps = total;
-    if (counts) for (auto &tc : tcounts) for (size_t k = 0; k < tc.size(); ++k) counts[k] += tc[k];
     return 0;
 }
 

@@ -1,0 +1,495 @@
+// trw_api.cu -- the extern "C" boundary of libtrw_gpu.so (include/trw.h).
+//
+// Owns the graph's HBM arrays, the static tables and the per-call engine
+// state, maps the reference's (app, mode, sampler) triple (types.h:41-59,
+// creeper.h:700-788) onto the two kernel families, and stages host buffers.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/trw.h"
+#include "trw_device.cuh"
+#include "trw_internal.h"
+
+using namespace trw;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define TRW_CUDA(call)                                                                             \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(TRW_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+bool is_device_ptr(const void *ptr) {
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Device allocation that frees itself.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t ensure(size_t want) {
+        if (bytes >= want) return cudaSuccess;
+        if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+};
+
+// One in-flight call's device state; reused once its event has completed.
+struct EngineSlot {
+    unsigned long long *queue_head = nullptr;  // points into the graph's state block
+    unsigned long long *steps = nullptr;
+    cudaEvent_t done = nullptr;
+    bool used = false;
+};
+
+constexpr int kEngineSlots = 64;
+
+int app_weight_kind(int app) {
+    switch (app) {
+    case TRW_APP_PPR: return kUnitWeight;
+    case TRW_APP_NODE2VEC: return kNode2Vec;
+    case TRW_APP_METAPATH: return kLabelSchema;
+    default: return kEdgeWeight;
+    }
+}
+
+}  // namespace
+
+struct trw_graph {
+    int device = 0;
+    int num_sms = 1;
+    int32_t n = 0;
+    int64_t e = 0;
+    int32_t max_degree = 0;
+    bool sorted = false;
+    int2 *rows = nullptr;
+    int32_t *adj = nullptr;
+    double *weight = nullptr;
+    int32_t *label = nullptr;
+    AliasSlot *alias = nullptr;
+    double *prefix = nullptr;
+    double *rmax = nullptr;
+    int alias_kind = -1, prefix_kind = -1, rmax_kind = -1;
+    // engine state block: [kEngineSlots x (queue, steps)] + error word
+    unsigned long long *state = nullptr;
+    int *error = nullptr;
+    EngineSlot slots[kEngineSlots];
+    int next_slot = 0;
+    DevBuf stage;
+    DevBuf alias_scratch;
+    cudaEvent_t scratch_done = nullptr;
+    LaunchShape shape[5];
+    std::mutex mu;
+};
+
+namespace {
+
+void destroy_graph(trw_graph *g) {
+    if (!g) return;
+    cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
+    cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state);
+    for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
+    if (g->scratch_done) cudaEventDestroy(g->scratch_done);
+    delete g;
+}
+
+DevGraph dev_view(const trw_graph *g) {
+    DevGraph d;
+    d.rows = g->rows; d.adj = g->adj; d.weight = g->weight; d.label = g->label;
+    d.alias = g->alias; d.prefix = g->prefix; d.rmax = g->rmax; d.n = g->n; d.e = g->e;
+    return d;
+}
+
+int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
+    const DevGraph d = dev_view(g);
+    if (kind == TRW_WEIGHTS_EDGE && !g->weight) return fail(TRW_ERR_INVALID, "edge weights were not supplied");
+    const int unit = kind == TRW_WEIGHTS_UNIT;
+    if (sampler == TRW_SAMPLER_ALIAS) {
+        if (!g->alias) TRW_CUDA(cudaMalloc(&g->alias, sizeof(AliasSlot) * (size_t)(g->e ? g->e : 1)));
+        TRW_CUDA(launch_build_alias(d, unit, g->alias, st));
+        g->alias_kind = kind;
+    } else if (sampler == TRW_SAMPLER_ITS) {
+        if (!g->prefix) TRW_CUDA(cudaMalloc(&g->prefix, sizeof(double) * (size_t)(g->e ? g->e : 1)));
+        TRW_CUDA(launch_build_prefix(d, unit, g->prefix, st));
+        g->prefix_kind = kind;
+    } else if (sampler == TRW_SAMPLER_REJECTION) {
+        if (!g->rmax) TRW_CUDA(cudaMalloc(&g->rmax, sizeof(double) * (size_t)g->n));
+        TRW_CUDA(launch_build_max(d, unit, g->rmax, st));
+        g->rmax_kind = kind;
+    } else {
+        return fail(TRW_ERR_INVALID, "sampler %d has no static table", sampler);
+    }
+    return TRW_OK;
+}
+
+// Call-local plan: which kernel family and template arguments run.
+struct Plan {
+    bool warp_family = false;
+    int sampler = kUniform;
+    int update = kFixedLength;
+    int weight_kind = kUnitWeight;
+    int table_kind = -1;  // static table weights the run needs
+};
+
+int make_plan(const trw_graph *g, const trw_walk_desc *d, Plan &pl) {
+    if (d->app < 0 || d->app > 4) return fail(TRW_ERR_INVALID, "unknown app %d", d->app);
+    pl.update = d->app == TRW_APP_PPR ? kGeometric : kFixedLength;
+    // length_ starts at 1 and is compared with l_ only after a move, so l_ < 2
+    // never ends (deepwalk.cpp:23-25); tp <= 0 never ends a PPR walk.
+    if (pl.update == kFixedLength && d->length < 2) return fail(TRW_ERR_INVALID, "walk length must be >= 2");
+    if (pl.update == kGeometric && !(d->tp >= 1e-6 && d->tp <= 1.0))
+        return fail(TRW_ERR_INVALID, "PPR termination probability must be in [1e-6, 1]");
+    if (d->app == TRW_APP_NODE2VEC && !(d->p > 0.0 && d->q > 0.0))
+        return fail(TRW_ERR_INVALID, "Node2Vec p and q must be positive");
+    const int wk = app_weight_kind(d->app);
+    if (d->app == TRW_APP_METAPATH) {
+        if (!g->label) return fail(TRW_ERR_INVALID, "MetaPath needs edge labels");
+        if (!d->schema || d->schema_len < 1 || d->schema_len > TRW_MAX_SCHEMA)
+            return fail(TRW_ERR_INVALID, "MetaPath schema length must be in [1, %d]", TRW_MAX_SCHEMA);
+    }
+    if (d->app == TRW_APP_NODE2VEC && !g->sorted)
+        return fail(TRW_ERR_GRAPH, "Node2Vec needs sorted neighbour lists (Graph::is_neighbor)");
+    switch (d->mode) {
+    case TRW_MODE_UNIFORM:  // uniform_compute ignores the sampler (creeper.h:780-782)
+        pl.sampler = kUniform;
+        return TRW_OK;
+    case TRW_MODE_STATIC:
+        if (d->app == TRW_APP_NODE2VEC || d->app == TRW_APP_METAPATH)
+            return fail(TRW_ERR_UNSUPPORTED, "static tables need walker-independent weights "
+                                             "(the reference gathers them with an uninitialised walker)");
+        if (d->sampler != TRW_SAMPLER_ITS && d->sampler != TRW_SAMPLER_ALIAS && d->sampler != TRW_SAMPLER_REJECTION)
+            return fail(TRW_ERR_UNSUPPORTED, "static mode supports ITS, alias and rejection sampling");
+        pl.sampler = d->sampler;
+        pl.table_kind = d->app == TRW_APP_PPR ? TRW_WEIGHTS_UNIT : TRW_WEIGHTS_EDGE;
+        if (pl.table_kind == TRW_WEIGHTS_EDGE && !g->weight) return fail(TRW_ERR_INVALID, "app needs edge weights");
+        return TRW_OK;
+    case TRW_MODE_DYNAMIC:
+        if (wk == kEdgeWeight && !g->weight) return fail(TRW_ERR_INVALID, "app needs edge weights");
+        pl.weight_kind = wk;
+        if (d->sampler == TRW_SAMPLER_MAXWEIGHT_REJECTION) {
+            if (d->app == TRW_APP_METAPATH)
+                return fail(TRW_ERR_UNSUPPORTED, "MetaPath with max-weight rejection never terminates on "
+                                                 "rows without a matching label");
+            pl.sampler = kMaxRejection;
+            return TRW_OK;
+        }
+        if (d->sampler == TRW_SAMPLER_ITS || d->sampler == TRW_SAMPLER_ALIAS || d->sampler == TRW_SAMPLER_REJECTION) {
+            pl.warp_family = true;
+            pl.sampler = d->sampler;
+            return TRW_OK;
+        }
+        return fail(TRW_ERR_UNSUPPORTED, "dynamic mode supports ITS, alias, rejection and max-weight rejection");
+    }
+    return fail(TRW_ERR_INVALID, "unknown mode %d", d->mode);
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Shared implementation of trw_walk and trw_ppr_batch.
+int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
+             int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
+             int32_t *lengths, int32_t *counts, int64_t counts_len, bool zero_counts, uint64_t *steps,
+             int32_t engine, cudaStream_t st) {
+    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
+    if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
+    if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
+    if (engine != TRW_ENGINE_PERSISTENT && engine != TRW_ENGINE_PLAIN) return fail(TRW_ERR_INVALID, "bad engine");
+    Plan pl;
+    int rc = make_plan(g, desc, pl);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    if (pl.table_kind >= 0) {
+        const int have = pl.sampler == kAlias ? g->alias_kind : pl.sampler == kITS ? g->prefix_kind : g->rmax_kind;
+        if (have != pl.table_kind) {  // compute() rebuilds its static tables each run (creeper.h:700-702)
+            rc = build_table(g, pl.sampler, pl.table_kind, st);
+            if (rc) return rc;
+        }
+    }
+
+    // Stage host buffers.
+    const bool h_src = sources && !is_device_ptr(sources);
+    const bool h_paths = paths && !is_device_ptr(paths);
+    const bool h_len = lengths && !is_device_ptr(lengths);
+    const bool h_cnt = counts && !is_device_ptr(counts);
+    const bool h_steps = steps && !is_device_ptr(steps);
+    const size_t b_src = h_src ? align_up(sizeof(int32_t) * (size_t)num_sources) : 0;
+    const size_t b_paths = h_paths ? align_up(sizeof(int32_t) * (size_t)num_walkers * (size_t)path_cap) : 0;
+    const size_t b_len = h_len ? align_up(sizeof(int32_t) * (size_t)num_walkers) : 0;
+    const size_t b_cnt = h_cnt ? align_up(sizeof(int32_t) * (size_t)counts_len) : 0;
+    const bool staged = b_src || b_paths || b_len || b_cnt;
+    if (staged) TRW_CUDA(g->stage.ensure(b_src + b_paths + b_len + b_cnt + 256));
+    char *base = static_cast<char *>(g->stage.p);
+    const int32_t *d_src = sources;
+    int32_t *d_paths = paths, *d_len = lengths, *d_cnt = counts;
+    if (h_src) {
+        d_src = reinterpret_cast<int32_t *>(base);
+        TRW_CUDA(cudaMemcpyAsync((void *)d_src, sources, sizeof(int32_t) * num_sources, cudaMemcpyHostToDevice, st));
+    }
+    base += b_src;
+    if (h_paths) d_paths = reinterpret_cast<int32_t *>(base);
+    base += b_paths;
+    if (h_len) d_len = reinterpret_cast<int32_t *>(base);
+    base += b_len;
+    if (h_cnt) {
+        d_cnt = reinterpret_cast<int32_t *>(base);
+        if (zero_counts) TRW_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(int32_t) * counts_len, st));
+        else TRW_CUDA(cudaMemcpyAsync(d_cnt, counts, sizeof(int32_t) * counts_len, cudaMemcpyHostToDevice, st));
+    } else if (counts && zero_counts) {
+        TRW_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(int32_t) * counts_len, st));
+    }
+
+    // Engine state slot (queue head + step counter), reused after its event.
+    EngineSlot &slot = g->slots[g->next_slot];
+    g->next_slot = (g->next_slot + 1) % kEngineSlots;
+    if (slot.used) TRW_CUDA(cudaEventSynchronize(slot.done));
+    TRW_CUDA(cudaMemsetAsync(slot.queue_head, 0, 2 * sizeof(unsigned long long), st));
+
+    WalkParams p;
+    std::memset(&p, 0, sizeof p);
+    p.g = dev_view(g);
+    p.length = desc->length;
+    p.schema_len = desc->app == TRW_APP_METAPATH ? desc->schema_len : 1;
+    if (desc->app == TRW_APP_METAPATH)
+        for (int i = 0; i < desc->schema_len; ++i) p.schema[i] = desc->schema[i];
+    // node2vec.cpp:176-178,227,234: weights 1/p (return), 1 (common neighbour), 1/q
+    p.p_w = desc->p != 0.0 ? 1.0 / desc->p : 0.0;
+    p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
+    p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
+    p.tp = desc->tp;
+    p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
+                 : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
+    p.seed = desc->seed;
+    p.static_unit = pl.table_kind == TRW_WEIGHTS_UNIT;
+    p.sources = d_src;
+    p.num_walkers = num_walkers;
+    p.per_query = per_query;
+    p.id_base = id_base;
+    p.paths = d_paths;
+    p.path_cap = paths ? path_cap : 0;
+    p.lengths = d_len;
+    p.counts = d_cnt;
+    p.queue_head = slot.queue_head;
+    p.steps = slot.steps;
+    p.error = g->error;
+
+    LaunchShape shape = g->shape[pl.sampler];
+    shape.engine = engine;
+    shape.num_sms = g->num_sms;
+    cudaError_t le;
+    if (pl.warp_family) {
+        if (pl.sampler == kAlias) {
+            // one raw + one table row of max_degree slots per warp, at most 1 GiB
+            const int64_t stride = 2 * (int64_t)std::max(1, g->max_degree);
+            int64_t warps = warp_engine_warps(p, shape);
+            const int64_t cap = (int64_t)((1ull << 30) / (sizeof(AliasSlot) * (uint64_t)stride));
+            if (warps > cap) warps = cap;
+            warps = std::max<int64_t>(8, warps / 8 * 8);
+            TRW_CUDA(g->alias_scratch.ensure(sizeof(AliasSlot) * (size_t)(warps * stride)));
+            p.alias_scratch = static_cast<AliasSlot *>(g->alias_scratch.p);
+            p.alias_scratch_stride = stride;
+            shape.max_warps = warps;
+            TRW_CUDA(cudaStreamWaitEvent(st, g->scratch_done, 0));
+        }
+        le = launch_walk_warp(p, pl.sampler, pl.update, pl.weight_kind, shape, st);
+        if (le == cudaSuccess && pl.sampler == kAlias) le = cudaEventRecord(g->scratch_done, st);
+    } else {
+        le = launch_walk_thread(p, pl.sampler, pl.update, pl.weight_kind, shape, st);
+    }
+    if (le != cudaSuccess) return fail(TRW_ERR_CUDA, "walk launch: %s", cudaGetErrorString(le));
+    if (steps) TRW_CUDA(cudaMemcpyAsync(steps, slot.steps, sizeof(uint64_t), h_steps ? cudaMemcpyDeviceToHost
+                                                                                      : cudaMemcpyDeviceToDevice, st));
+    if (h_paths) TRW_CUDA(cudaMemcpyAsync(paths, d_paths, sizeof(int32_t) * (size_t)num_walkers * path_cap,
+                                          cudaMemcpyDeviceToHost, st));
+    if (h_len) TRW_CUDA(cudaMemcpyAsync(lengths, d_len, sizeof(int32_t) * (size_t)num_walkers, cudaMemcpyDeviceToHost, st));
+    if (h_cnt) TRW_CUDA(cudaMemcpyAsync(counts, d_cnt, sizeof(int32_t) * (size_t)counts_len, cudaMemcpyDeviceToHost, st));
+    TRW_CUDA(cudaEventRecord(slot.done, st));
+    slot.used = true;
+    if (staged || h_steps) {
+        TRW_CUDA(cudaStreamSynchronize(st));
+        int err = 0;
+        TRW_CUDA(cudaMemcpy(&err, g->error, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            TRW_CUDA(cudaMemset(g->error, 0, sizeof(int)));
+            return fail(TRW_ERR_DEVICE, "device error word %d (1 = rejection trial limit, 2 = invalid source vertex)", err);
+        }
+    }
+    return TRW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t trw_version(void) { return 1000; }
+
+const char *trw_last_error(void) { return g_last_error.c_str(); }
+
+int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *weight, const int32_t *label,
+                     int32_t n, int64_t e, uint32_t flags, trw_graph **out) {
+    if (!out) return fail(TRW_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (n <= 0 || e < 0 || !row_ptr || (e > 0 && !adj)) return fail(TRW_ERR_INVALID, "bad CSR arguments");
+    if (e >= (int64_t)1 << 31) return fail(TRW_ERR_CAPACITY, "e = %lld: this build stores int32 row offsets (e < 2^31)",
+                                           (long long)e);
+    trw_graph *g = new trw_graph();
+    auto bail = [&](int code) { destroy_graph(g); return code; };
+    if (cudaGetDevice(&g->device) != cudaSuccess) return bail(fail(TRW_ERR_CUDA, "no CUDA device"));
+    cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device);
+    g->n = n;
+    g->e = e;
+    const size_t es = (size_t)(e ? e : 1);
+    int64_t *d_row = nullptr;
+    int *d_flags = nullptr;
+    cudaError_t ce = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (ce == cudaSuccess) ce = x; };
+    chk(cudaMalloc(&g->rows, sizeof(int2) * (size_t)n));
+    chk(cudaMalloc(&g->adj, sizeof(int32_t) * es));
+    chk(cudaMalloc(&d_row, sizeof(int64_t) * ((size_t)n + 1)));
+    chk(cudaMalloc(&d_flags, 3 * sizeof(int)));
+    if (weight) chk(cudaMalloc(&g->weight, sizeof(double) * es));
+    if (label) chk(cudaMalloc(&g->label, sizeof(int32_t) * es));
+    chk(cudaMalloc(&g->state, sizeof(unsigned long long) * (2 * kEngineSlots + 1)));
+    if (ce != cudaSuccess) { cudaFree(d_row); cudaFree(d_flags); return bail(fail(TRW_ERR_CUDA, "graph allocation: %s", cudaGetErrorString(ce))); }
+    g->error = reinterpret_cast<int *>(g->state + 2 * kEngineSlots);
+    for (int i = 0; i < kEngineSlots; ++i) {
+        g->slots[i].queue_head = g->state + 2 * i;
+        g->slots[i].steps = g->state + 2 * i + 1;
+        chk(cudaEventCreateWithFlags(&g->slots[i].done, cudaEventDisableTiming));
+    }
+    chk(cudaEventCreateWithFlags(&g->scratch_done, cudaEventDisableTiming));
+    chk(cudaMemset(g->state, 0, sizeof(unsigned long long) * (2 * kEngineSlots + 1)));
+    chk(cudaMemcpy(d_row, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDefault));
+    if (e) chk(cudaMemcpy(g->adj, adj, sizeof(int32_t) * (size_t)e, cudaMemcpyDefault));
+    if (weight && e) chk(cudaMemcpy(g->weight, weight, sizeof(double) * (size_t)e, cudaMemcpyDefault));
+    if (label && e) chk(cudaMemcpy(g->label, label, sizeof(int32_t) * (size_t)e, cudaMemcpyDefault));
+    chk(cudaMemset(d_flags, 0, 3 * sizeof(int)));
+    // pass 1 without the sortedness check decides validity; pass 2 records sortedness
+    if (ce == cudaSuccess) ce = launch_validate_graph(d_row, g->adj, n, e, 0, g->rows, d_flags, d_flags + 1, 0);
+    if (ce == cudaSuccess) ce = launch_validate_graph(d_row, g->adj, n, e, 1, g->rows, d_flags + 2, d_flags + 1, 0);
+    int hf[3] = {0, 0, 0};
+    chk(cudaMemcpy(hf, d_flags, sizeof hf, cudaMemcpyDeviceToHost));
+    cudaFree(d_row);
+    cudaFree(d_flags);
+    if (ce != cudaSuccess) return bail(fail(TRW_ERR_CUDA, "graph upload: %s", cudaGetErrorString(ce)));
+    if (hf[0]) return bail(fail(TRW_ERR_GRAPH, "invalid CSR (flags %d: 1 offsets, 2 monotonicity, 4 vertex id range)", hf[0]));
+    g->sorted = (hf[2] & 8) == 0;
+    if ((flags & TRW_GRAPH_CHECK_SORTED) && !g->sorted) return bail(fail(TRW_ERR_GRAPH, "neighbour lists are not sorted"));
+    g->max_degree = hf[1];
+    *out = g;
+    return TRW_OK;
+}
+
+int trw_graph_destroy(trw_graph *g) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    cudaSetDevice(g->device);
+    cudaDeviceSynchronize();
+    destroy_graph(g);
+    return TRW_OK;
+}
+
+int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degree) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    if (n) *n = g->n;
+    if (e) *e = g->e;
+    if (max_degree) *max_degree = g->max_degree;
+    return TRW_OK;
+}
+
+int trw_tables_build(trw_graph *g, int32_t sampler, int32_t weight_kind, trw_stream_t stream) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    if (weight_kind != TRW_WEIGHTS_EDGE && weight_kind != TRW_WEIGHTS_UNIT) return fail(TRW_ERR_INVALID, "bad weight kind");
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    return build_table(g, sampler, weight_kind, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t out_bytes) {
+    if (!g || !out) return fail(TRW_ERR_INVALID, "null argument");
+    const void *src = nullptr;
+    size_t bytes = 0;
+    if (sampler == TRW_SAMPLER_ALIAS) { src = g->alias; bytes = sizeof(AliasSlot) * (size_t)g->e; }
+    else if (sampler == TRW_SAMPLER_ITS) { src = g->prefix; bytes = sizeof(double) * (size_t)g->e; }
+    else if (sampler == TRW_SAMPLER_REJECTION) { src = g->rmax; bytes = sizeof(double) * (size_t)g->n; }
+    else return fail(TRW_ERR_INVALID, "sampler %d has no static table", sampler);
+    if (!src) return fail(TRW_ERR_NO_TABLES, "table not built");
+    if (out_bytes < bytes) return fail(TRW_ERR_CAPACITY, "output holds %zu bytes, table needs %zu", out_bytes, bytes);
+    TRW_CUDA(cudaSetDevice(g->device));
+    TRW_CUDA(cudaDeviceSynchronize());
+    TRW_CUDA(cudaMemcpy(out, src, bytes, cudaMemcpyDefault));
+    return TRW_OK;
+}
+
+int trw_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_walkers, int64_t id_base,
+             int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts, uint64_t *steps, int32_t engine,
+             trw_stream_t stream) {
+    return run_walk(g, desc, sources, num_walkers, num_walkers, 0, id_base, paths, path_cap, lengths, counts,
+                    g ? (int64_t)g->n : 0, false, steps, engine, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
+                  int64_t walkers_per_query, int32_t *counts, uint64_t *steps, uint32_t flags, int32_t engine,
+                  trw_stream_t stream) {
+    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
+    if (num_queries < 0 || walkers_per_query <= 0) return fail(TRW_ERR_INVALID, "bad batch shape");
+    if (desc->app != TRW_APP_PPR) return fail(TRW_ERR_INVALID, "trw_ppr_batch runs the PPR app");
+    return run_walk(g, desc, sources, num_queries, num_queries * walkers_per_query, walkers_per_query, 0, nullptr, 0,
+                    nullptr, counts, num_queries * (int64_t)g->n, (flags & TRW_PPR_ZERO_COUNTS) != 0, steps, engine,
+                    reinterpret_cast<cudaStream_t>(stream));
+}
+
+int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm) {
+    if (!g || sampler < 0 || sampler > 4) return fail(TRW_ERR_INVALID, "bad arguments");
+    if (walkers_per_thread != 0 && walkers_per_thread != 1 && walkers_per_thread != 2 && walkers_per_thread != 4 &&
+        walkers_per_thread != 8)
+        return fail(TRW_ERR_INVALID, "walkers per thread must be 1, 2, 4 or 8");
+    std::lock_guard<std::mutex> lock(g->mu);
+    g->shape[sampler].ring = walkers_per_thread ? walkers_per_thread : 4;
+    g->shape[sampler].ctas_per_sm = ctas_per_sm > 0 ? ctas_per_sm : 0;
+    return TRW_OK;
+}
+
+int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_per_thread, int32_t *ctas_per_sm) {
+    if (!g || sampler < 0 || sampler > 4) return fail(TRW_ERR_INVALID, "bad arguments");
+    if (walkers_per_thread) *walkers_per_thread = g->shape[sampler].ring;
+    if (ctas_per_sm) *ctas_per_sm = g->shape[sampler].ctas_per_sm;
+    return TRW_OK;
+}
+
+int trw_device_error(trw_graph *g, int32_t *code) {
+    if (!g || !code) return fail(TRW_ERR_INVALID, "null argument");
+    TRW_CUDA(cudaSetDevice(g->device));
+    TRW_CUDA(cudaDeviceSynchronize());
+    int v = 0;
+    TRW_CUDA(cudaMemcpy(&v, g->error, sizeof(int), cudaMemcpyDeviceToHost));
+    TRW_CUDA(cudaMemset(g->error, 0, sizeof(int)));
+    *code = v;
+    return TRW_OK;
+}
+
+}  // extern "C"

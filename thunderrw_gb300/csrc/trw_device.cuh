@@ -1,0 +1,178 @@
+// trw_device.cuh -- device-side building blocks shared by the walk and
+// table-builder kernels: Philox4x32-10, SFMT's u32->double conversions, the
+// HBM graph view, the app hooks and the launch parameters.
+//
+// All translation units including this header are compiled with
+// --fmad=false: every double operation is one IEEE round-to-nearest op, the
+// same arithmetic as the reference's x86-64 build.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace trw {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11).  key = seed; counter = (block, step,
+// walker lo, walker hi).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+constexpr uint32_t kTermBlock = 0x80000000u;
+
+__device__ __forceinline__ uint4 draw_block(uint64_t seed, uint64_t walker, uint32_t step, uint32_t block) {
+    return philox4x32_10(make_uint4(block, step, (uint32_t)walker, (uint32_t)(walker >> 32)),
+                         (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+__device__ __forceinline__ uint32_t word(const uint4 &v, uint32_t i) {
+    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Sequential draws of one (walker, step) move: draw d is word d%4 of block d/4.
+struct DrawCursor {
+    uint64_t seed, walker;
+    uint32_t step, draw;
+    uint4 buf;
+    __device__ __forceinline__ DrawCursor(uint64_t s, uint64_t w, uint32_t st, const uint4 &first)
+        : seed(s), walker(w), step(st), draw(0), buf(first) {}
+    __device__ __forceinline__ uint32_t next() {
+        if (draw && (draw & 3) == 0) buf = draw_block(seed, walker, step, draw >> 2);
+        return word(buf, draw++ & 3);
+    }
+};
+
+// SFMT.h:193-228: real1 = v / (2^32 - 1) via the rounded reciprocal, real2 = v * 2^-32.
+__device__ __forceinline__ double real1(uint32_t v) { return (double)v * (1.0 / 4294967295.0); }
+__device__ __forceinline__ double real2(uint32_t v) { return (double)v * (1.0 / 4294967296.0); }
+
+// ---------------------------------------------------------------------------
+// Graph view in HBM.
+//   rows[v]  = (row_ptr[v], row_ptr[v+1]) as one 8-byte pair: a single aligned
+//              load per step (the offset_pair_ of graph.cpp:86-91 at half size)
+//   adj      = neighbour ids, sorted per row
+//   alias    = 16-byte AliasSlot rows, one aligned 16-byte load per draw
+// ---------------------------------------------------------------------------
+struct AliasSlot {
+    double prob;
+    int32_t first;
+    int32_t second;
+};
+static_assert(sizeof(AliasSlot) == 16, "AliasSlot must be 16 bytes");
+
+struct DevGraph {
+    const int2 *rows;
+    const int32_t *adj;
+    const double *weight;
+    const int32_t *label;
+    const AliasSlot *alias;
+    const double *prefix;
+    const double *rmax;
+    int32_t n;
+    int64_t e;
+};
+
+enum Sampler : int { kUniform = 0, kITS = 1, kAlias = 2, kRejection = 3, kMaxRejection = 4 };
+enum Update : int { kFixedLength = 0, kGeometric = 1 };
+enum WeightKind : int { kEdgeWeight = 0, kUnitWeight = 1, kNode2Vec = 2, kLabelSchema = 3 };
+
+constexpr int kMaxSchema = 64;
+constexpr uint32_t kMaxTrials = 1u << 20;
+
+enum DeviceError : int { kErrTrials = 1, kErrVertex = 2 };
+
+struct WalkParams {
+    DevGraph g;
+    // app
+    int32_t length;       // l_
+    int32_t schema_len;
+    double p_w, q_w, n2v_max, tp, max_weight;
+    uint64_t seed;
+    int32_t static_unit;  // static rejection with unit weights (PPR)
+    int32_t schema[kMaxSchema];
+    // walkers
+    const int32_t *sources;
+    int64_t num_walkers;
+    int64_t per_query;    // > 0: walker i starts at sources[i / per_query]
+    int64_t id_base;
+    // outputs
+    int32_t *paths;
+    int32_t path_cap;
+    int32_t *lengths;
+    int32_t *counts;
+    // engine state
+    unsigned long long *queue_head;
+    unsigned long long *steps;
+    int *error;
+    // dynamic alias scratch: one table of max_degree slots per warp
+    AliasSlot *alias_scratch;
+    int64_t alias_scratch_stride;
+};
+
+// Graph::is_neighbor (graph.h:180-199): binary search for the higher-degree
+// endpoint in the lower-degree endpoint's sorted list (ties search u in v's).
+__device__ __forceinline__ bool is_neighbor(const DevGraph &g, int32_t u, int2 ru, int32_t v, int2 rv) {
+    int32_t du = ru.y - ru.x, dv = rv.y - rv.x;
+    if (du < dv) { int32_t t = u; u = v; v = t; int2 tr = ru; ru = rv; rv = tr; }
+    const int32_t *nb = g.adj + rv.x;
+    int32_t lo = 0, hi = rv.y - rv.x - 1;
+    while (lo <= hi) {
+        const int32_t mid = lo + ((hi - lo) >> 1);
+        const int32_t x = __ldg(nb + mid);
+        if (x == u) return true;
+        if (x > u) hi = mid - 1; else lo = mid + 1;
+    }
+    return false;
+}
+
+// The weight hook of the app (node2vec.cpp:182-196, metapath.cpp:22-30,
+// deepwalk.cpp:19-21, ppr.cpp:95-97) for the edge (cur -> nbr) at eid.
+// `len` and `prev` are the walker's length_ and seq_[length_-2].
+template <int WK>
+__device__ __forceinline__ double app_weight(const WalkParams &p, int32_t len, int32_t prev, int2 prev_row,
+                                             int32_t nbr, int64_t eid) {
+    if (WK == kEdgeWeight) return __ldg(p.g.weight + eid);
+    if (WK == kUnitWeight) return 1.0;
+    if (WK == kLabelSchema) return __ldg(p.g.label + eid) != p.schema[(len - 1) % p.schema_len] ? 0.0 : 1.0;
+    // Node2Vec
+    if (len == 1) return p.n2v_max;
+    if (nbr == prev) return p.p_w;
+    const int2 rn = __ldg(p.g.rows + nbr);
+    return is_neighbor(p.g, prev, prev_row, nbr, rn) ? 1.0 : p.q_w;
+}
+
+// The update hook: length_ == l_, or PPR's real1(termination draw) <= tp.
+template <int U>
+__device__ __forceinline__ bool app_update(const WalkParams &p, uint64_t wid, int32_t len) {
+    if (U == kFixedLength) return len == p.length;
+    const uint4 t = draw_block(p.seed, wid, (uint32_t)len, kTermBlock);
+    return real1(t.x) <= p.tp;
+}
+
+// Utility::upper_bound_branchless (utility.h:18-27): number of entries <= t.
+__device__ __forceinline__ int32_t upper_bound_bl(const double *src, int32_t n, double t) {
+    const double *base = src;
+    while (n > 1) {
+        const int32_t half = n >> 1;
+        base = (__ldg(base + half) <= t) ? base + half : base;
+        n -= half;
+    }
+    return (int32_t)((__ldg(base) <= t) + (base - src));
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+}  // namespace trw

@@ -1,0 +1,37 @@
+// trw_internal.h -- host-side declarations shared by the library's
+// translation units (not part of the public ABI; see include/trw.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "trw_device.cuh"
+
+namespace trw {
+
+constexpr int kThreadBlock = 256;
+constexpr int kEnginePersistent = 0;
+constexpr int kEnginePlain = 1;
+
+struct LaunchShape {
+    int engine = kEnginePersistent;
+    int ring = 4;         // walkers in flight per lane (thread family)
+    int ctas_per_sm = 0;  // 0 = as many as fit
+    int num_sms = 1;
+    int64_t max_warps = 0;  // dynamic alias: warps with a scratch table
+};
+
+cudaError_t launch_walk_thread(const WalkParams &p, int sampler, int update, int weight_kind,
+                               const LaunchShape &shape, cudaStream_t st);
+cudaError_t launch_walk_warp(const WalkParams &p, int sampler, int update, int weight_kind,
+                             const LaunchShape &shape, cudaStream_t st);
+// number of per-warp dynamic-alias scratch tables the warp engine will use
+int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
+
+cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
+cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);
+cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st);
+cudaError_t launch_validate_graph(const int64_t *row, const int32_t *adj, int32_t n, int64_t e, int check_sorted,
+                                  int2 *rows_out, int *bad, int *max_degree, cudaStream_t st);
+
+}  // namespace trw

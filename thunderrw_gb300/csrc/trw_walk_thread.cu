@@ -1,0 +1,331 @@
+// trw_walk_thread.cu -- walk kernels where each lane owns its walkers:
+// Uniform (uniform_sampling.h), static Alias (alias_sampling.h:69-106,147-172),
+// static ITS (inverse_transformation_sampling.h:36-145,259-286), static
+// Rejection (rejection_sampling.h:28-137,334-366) and dynamic max-weight
+// Rejection (rejection_sampling.h:139-230,368-402 with MaxRSFrame,
+// rs_frame.h:47-83), under the Gather-Move-Update loop of creeper.h:336-541.
+//
+// Persistent engine: a grid of (SM count x CTAs/SM) CTAs; every lane keeps R
+// walkers in flight (the GPU analogue of the reference's RING_SIZE ring,
+// types.h:21) and runs each step stage for all R walkers before the next
+// stage, so a lane has R independent random loads outstanding per stage.  A
+// lane whose walker finishes takes the next walker id from its warp's
+// reservoir, refilled by one atomicAdd per kChunk walkers on a global queue
+// head (the admission of creeper.h:321-332).
+//
+// Plain engine: one thread per walker, walker = global thread id, no refill.
+#include "trw_device.cuh"
+#include "trw_internal.h"
+
+namespace trw {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Slot {
+    int64_t widx;   // walker index in the call, -1 = empty
+    int64_t cbase;  // visit-count row offset (query * n)
+    int32_t cur, prev, len;
+    int2 crow, prow;  // row pairs of cur and prev
+};
+
+__device__ __forceinline__ void finish(const WalkParams &p, Slot &s) {
+    if (p.lengths) p.lengths[s.widx] = s.len;
+    if (p.paths) {
+        int32_t *row = p.paths + s.widx * (int64_t)p.path_cap;
+        for (int32_t k = s.len; k < p.path_cap; ++k) row[k] = -1;
+    }
+    s.widx = -1;
+}
+
+__device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx) {
+    int64_t q = 0;
+    int32_t src;
+    if (p.per_query > 0) { q = idx / p.per_query; src = __ldg(p.sources + q); }
+    else src = __ldg(p.sources + idx);
+    s.widx = idx;
+    s.cbase = q * (int64_t)p.g.n;
+    s.len = 1;
+    s.prev = -1;
+    s.prow = make_int2(0, 0);
+    if (p.paths && p.path_cap > 0) p.paths[idx * (int64_t)p.path_cap] = src;
+    if (src < 0 || src >= p.g.n) {  // rejected here so no kernel reads outside the graph
+        atomicOr(p.error, kErrVertex);
+        s.cur = 0;
+        finish(p, s);
+        return;
+    }
+    s.cur = src;
+}
+
+__device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(a));
+    AliasSlot s;
+    s.prob = __hiloint2double(v.y, v.x);
+    s.first = v.z;
+    s.second = v.w;
+    return s;
+}
+
+// One step for each of the R slots, stage by stage.
+template <int S, int U, int WK, int R>
+__device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uint64_t &steps) {
+    const DevGraph &g = p.g;
+    int32_t nxt[R];
+    bool moved[R];
+    uint4 rnd[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        moved[r] = false;
+        nxt[r] = 0;
+        if (s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        if (s[r].widx >= 0) rnd[r] = draw_block(p.seed, (uint64_t)(p.id_base + s[r].widx), (uint32_t)s[r].len, 0);
+
+    if (S == kUniform) {
+        // uniform_interleaving_move (uniform_sampling.h:11-45)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (s[r].widx < 0) continue;
+            const int32_t deg = s[r].crow.y - s[r].crow.x;
+            if (deg > 0) { nxt[r] = __ldg(g.adj + s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg)); moved[r] = true; }
+        }
+    } else if (S == kAlias) {
+        // static_alias_interleaving_move (alias_sampling.h:221-258)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (s[r].widx < 0) continue;
+            const int32_t deg = s[r].crow.y - s[r].crow.x;
+            if (deg > 0) {
+                const AliasSlot a = load_alias(g.alias + s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg));
+                nxt[r] = real2(rnd[r].y) <= a.prob ? a.first : a.second;
+                moved[r] = true;
+            }
+        }
+    } else if (S == kITS) {
+        // static_its_interleaving_move (inverse_transformation_sampling.h:36-145):
+        // target = real2 * P[last], then the branchless upper bound of
+        // utility.h:18-27 advanced one probe per ring slot per round.
+        double t[R];
+        const double *base[R];
+        int32_t n[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            n[r] = 0;
+            if (s[r].widx < 0) continue;
+            const int32_t deg = s[r].crow.y - s[r].crow.x;
+            if (deg <= 0) continue;
+            const double total = __ldg(g.prefix + s[r].crow.y - 1);
+            if (total == 0.0) continue;  // zero-weight row: the walker stops
+            t[r] = real2(rnd[r].x) * total;
+            base[r] = g.prefix + s[r].crow.x;
+            n[r] = deg;
+        }
+        bool more = true;
+        while (more) {
+            more = false;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (n[r] > 1) {
+                    const int32_t half = n[r] >> 1;
+                    base[r] = (__ldg(base[r] + half) <= t[r]) ? base[r] + half : base[r];
+                    n[r] -= half;
+                    more |= n[r] > 1;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (n[r] == 1) {
+                const int32_t sel = (int32_t)((__ldg(base[r]) <= t[r]) + (base[r] - (g.prefix + s[r].crow.x)));
+                nxt[r] = __ldg(g.adj + s[r].crow.x + sel);
+                moved[r] = true;
+            }
+        }
+    } else if (S == kRejection) {
+        // static_rs_move (rejection_sampling.h:334-366): trial k uses draws 2k, 2k+1.
+        double mx[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (s[r].widx >= 0) mx[r] = __ldg(g.rmax + s[r].cur);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (s[r].widx < 0) continue;
+            const int32_t deg = s[r].crow.y - s[r].crow.x;
+            if (deg <= 0) continue;
+            DrawCursor c(p.seed, (uint64_t)(p.id_base + s[r].widx), (uint32_t)s[r].len, rnd[r]);
+            uint32_t trials = 0;
+            int32_t p0;
+            for (;;) {
+                p0 = (int32_t)(c.next() % (uint32_t)deg);
+                const double y = real2(c.next()) * mx[r];
+                const double w = p.static_unit ? 1.0 : __ldg(g.weight + s[r].crow.x + p0);
+                if (y <= w) break;
+                if (++trials >= kMaxTrials) break;
+            }
+            if (trials >= kMaxTrials) { atomicOr(p.error, kErrTrials); continue; }
+            nxt[r] = __ldg(g.adj + s[r].crow.x + p0);
+            moved[r] = true;
+        }
+    } else {
+        // dynamic max-weight rejection: dr_ = max_weight (creeper.h:648-653), then
+        // per trial position, app weight, real2 * max (rejection_sampling.h:368-402).
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (s[r].widx < 0) continue;
+            const int32_t deg = s[r].crow.y - s[r].crow.x;
+            if (deg <= 0) continue;
+            DrawCursor c(p.seed, (uint64_t)(p.id_base + s[r].widx), (uint32_t)s[r].len, rnd[r]);
+            uint32_t trials = 0;
+            int32_t nb;
+            for (;;) {
+                const int32_t p0 = (int32_t)(c.next() % (uint32_t)deg);
+                nb = __ldg(g.adj + s[r].crow.x + p0);
+                const double w = app_weight<WK>(p, s[r].len, s[r].prev, s[r].prow, nb, s[r].crow.x + p0);
+                const double y = real2(c.next()) * p.max_weight;
+                if (y <= w) break;
+                if (++trials >= kMaxTrials) break;
+            }
+            if (trials >= kMaxTrials) { atomicOr(p.error, kErrTrials); continue; }
+            nxt[r] = nb;
+            moved[r] = true;
+        }
+    }
+
+    // Move bookkeeping (e.g. alias_sampling.h:251-255) and update
+    // (creeper.h:299-319).
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (s[r].widx < 0) continue;
+        if (!moved[r]) { finish(p, s[r]); continue; }
+        s[r].prev = s[r].cur;
+        s[r].prow = s[r].crow;
+        s[r].cur = nxt[r];
+        if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
+        s[r].len += 1;
+        steps += 1;
+        if (p.counts) atomicAdd(p.counts + s[r].cbase + nxt[r], 1);
+        if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) finish(p, s[r]);
+    }
+}
+
+__device__ __forceinline__ void flush_steps(const WalkParams &p, uint64_t steps) {
+    unsigned long long v = steps;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.steps, v);
+}
+
+template <int S, int U, int WK, int R>
+__global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams p) {
+    const int lane = threadIdx.x & 31;
+    constexpr unsigned long long kChunk = 32ull * R * 2;
+    Slot s[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[r].widx = -1;
+    uint64_t steps = 0;
+    unsigned long long res_next = 0, res_end = 0;
+    bool drained = false;
+    for (;;) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            unsigned need = __ballot_sync(kFull, s[r].widx < 0);
+            while (need && !drained) {
+                if (res_next >= res_end) {
+                    unsigned long long b = 0;
+                    if (lane == 0) b = atomicAdd(p.queue_head, kChunk);
+                    b = __shfl_sync(kFull, b, 0);
+                    if (b >= (unsigned long long)p.num_walkers) { drained = true; break; }
+                    res_next = b;
+                    res_end = min(b + kChunk, (unsigned long long)p.num_walkers);
+                }
+                const unsigned avail = (unsigned)min(res_end - res_next, 32ull);
+                const unsigned rank = __popc(need & lanemask_lt());
+                const bool mine = ((need >> lane) & 1u) && rank < avail;
+                if (mine) admit(p, s[r], (int64_t)(res_next + rank));
+                res_next += min((unsigned)__popc(need), avail);
+                need &= ~__ballot_sync(kFull, mine);
+            }
+        }
+        bool live = false;
+#pragma unroll
+        for (int r = 0; r < R; ++r) live |= s[r].widx >= 0;
+        if (!__any_sync(kFull, live)) break;
+        step_ring<S, U, WK, R>(p, s, steps);
+    }
+    flush_steps(p, steps);
+}
+
+template <int S, int U, int WK>
+__global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t steps = 0;
+    if (idx < p.num_walkers) {
+        Slot s[1];
+        admit(p, s[0], idx);
+        while (s[0].widx >= 0) step_ring<S, U, WK, 1>(p, s, steps);
+    }
+    flush_steps(p, steps);
+}
+
+template <class K>
+int max_occupancy(K kernel) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kThreadBlock, 0) != cudaSuccess || n <= 0) n = 1;
+    return n;
+}
+
+template <int S, int U, int WK, int R>
+cudaError_t launch_persistent(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
+    static const int max_occ = max_occupancy(walk_persistent<S, U, WK, R>);
+    const int per_sm = shape.ctas_per_sm > 0 ? min(shape.ctas_per_sm, max_occ) : max_occ;
+    int64_t grid = (int64_t)shape.num_sms * per_sm;
+    const int64_t useful = (p.num_walkers + (int64_t)kThreadBlock * R - 1) / ((int64_t)kThreadBlock * R);
+    if (useful < grid) grid = useful;
+    if (grid <= 0) return cudaSuccess;
+    walk_persistent<S, U, WK, R><<<(unsigned)grid, kThreadBlock, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+template <int S, int U, int WK>
+cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
+    if (shape.engine == kEnginePlain) {
+        const int64_t blocks = (p.num_walkers + kThreadBlock - 1) / kThreadBlock;
+        if (blocks <= 0) return cudaSuccess;
+        walk_plain<S, U, WK><<<(unsigned)blocks, kThreadBlock, 0, st>>>(p);
+        return cudaGetLastError();
+    }
+    switch (shape.ring) {
+    case 1: return launch_persistent<S, U, WK, 1>(p, shape, st);
+    case 2: return launch_persistent<S, U, WK, 2>(p, shape, st);
+    case 8: return launch_persistent<S, U, WK, 8>(p, shape, st);
+    default: return launch_persistent<S, U, WK, 4>(p, shape, st);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_walk_thread(const WalkParams &p, int sampler, int update, int weight_kind,
+                               const LaunchShape &shape, cudaStream_t st) {
+    const bool geo = update == kGeometric;
+    switch (sampler) {
+    case kUniform: return geo ? launch_shape<kUniform, kGeometric, kUnitWeight>(p, shape, st)
+                              : launch_shape<kUniform, kFixedLength, kUnitWeight>(p, shape, st);
+    case kAlias: return geo ? launch_shape<kAlias, kGeometric, kUnitWeight>(p, shape, st)
+                            : launch_shape<kAlias, kFixedLength, kUnitWeight>(p, shape, st);
+    case kITS: return geo ? launch_shape<kITS, kGeometric, kUnitWeight>(p, shape, st)
+                          : launch_shape<kITS, kFixedLength, kUnitWeight>(p, shape, st);
+    case kRejection: return geo ? launch_shape<kRejection, kGeometric, kUnitWeight>(p, shape, st)
+                                : launch_shape<kRejection, kFixedLength, kUnitWeight>(p, shape, st);
+    case kMaxRejection:
+        if (weight_kind == kNode2Vec) return launch_shape<kMaxRejection, kFixedLength, kNode2Vec>(p, shape, st);
+        if (weight_kind == kEdgeWeight) return launch_shape<kMaxRejection, kFixedLength, kEdgeWeight>(p, shape, st);
+        if (geo) return launch_shape<kMaxRejection, kGeometric, kUnitWeight>(p, shape, st);
+        return cudaErrorInvalidValue;
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace trw
