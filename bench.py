@@ -143,7 +143,8 @@ def build_inputs(wl, args, device):
         out["per_query"] = wl["per_query"]
     else:
         out["sources"] = G.all_sources(g["row"], seed=0)
-    torch.cuda.synchronize()
+    if torch.device(device).type == "cuda":
+        torch.cuda.synchronize()
     return out
 
 
@@ -155,16 +156,17 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
     ncores = threads or os.cpu_count()
     if wl_name == "ppr":
         d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=wl["tp"], seed=11)
-        chunk = 16  # queries per pass; each pass zeroes and fills a 16 x N count block
+        chunk = 64  # queries per pass; each pass zeroes and fills a chunk x N count block
         counts = np.zeros((chunk, og.n), dtype=np.int32)
+        counts.fill(1)  # touch every page once, outside the timed passes
         total_steps, total_t, done_q = 0, 0.0, 0
         src = np.asarray(sources, dtype=np.int32)
         while total_t < seconds and done_q < src.size:
             qs = src[done_q:done_q + chunk]
             t0 = time.perf_counter()
             counts[: qs.size].fill(0)
-            r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_counts=True,
-                       want_lengths=False, num_queries=chunk, threads=ncores, interleaved=True, ring=64)
+            r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_lengths=False,
+                       num_queries=qs.size, threads=ncores, interleaved=True, ring=64, out_counts=counts)
             total_t += time.perf_counter() - t0
             total_steps += r["steps"]
             done_q += qs.size
@@ -393,12 +395,14 @@ def run_ours(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic_per_step.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            tv = json.load(f).get(args.workload)
-        if tv:
-            traffic = tv * steps_per_batch
+    # DRAM bytes per step from the committed ncu summary of the same kernel,
+    # scaled to this launch by its step count
+    import glob
+    import re
+    for md in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        m = re.search(r"traffic_bytes_per_step_%s = ([0-9.]+)" % args.workload, open(md).read())
+        if m:
+            traffic = float(m.group(1)) * steps_per_batch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "bytes_per_step": bps, "kernel_ms": kmean * 1e3,
             "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}

@@ -137,14 +137,20 @@ def draw_u32(seed, walker, step, d):
 
 
 def walk(graph: Graph, desc, sources, per_query=0, id_base=0, path_cap=0, want_lengths=True,
-         want_counts=False, num_queries=None, threads=0, interleaved=False, ring=64):
-    """Runs the oracle walks; returns dict(paths, lengths, counts, steps)."""
+         want_counts=False, num_queries=None, threads=0, interleaved=False, ring=64, out_counts=None):
+    """Runs the oracle walks; returns dict(paths, lengths, counts, steps).
+    ``out_counts`` (int32, C-contiguous, num_queries x n) receives the visit
+    counts added in place instead of a fresh array."""
     src = as_np(sources, np.int32)
     W = src.size * per_query if per_query > 0 else src.size
     paths = np.full((W, path_cap), -1, dtype=np.int32) if path_cap > 0 else None
     lengths = np.zeros(W, dtype=np.int32) if want_lengths else None
     nq = (src.size if per_query > 0 else 1) if num_queries is None else num_queries
-    counts = np.zeros((nq, graph.n), dtype=np.int32) if want_counts else None
+    if out_counts is not None:
+        assert out_counts.dtype == np.int32 and out_counts.flags.c_contiguous and out_counts.size >= nq * graph.n
+        counts = out_counts
+    else:
+        counts = np.zeros((nq, graph.n), dtype=np.int32) if want_counts else None
     steps = ctypes.c_uint64(0)
     g = graph.struct()
     if interleaved:
