@@ -174,6 +174,29 @@ int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thre
 int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_per_thread,
                          int32_t *ctas_per_sm);
 
+/* Dynamic-mode alias walks (TRW_MODE_DYNAMIC + TRW_SAMPLER_ALIAS, any app)
+ * that allocate nothing: no cudaMalloc, cudaFree or allocating library call.
+ * No counterpart in the reference; it is for callers that cannot allocate
+ * device memory while they walk (a framework that owns every device byte
+ * through its own pool, serving threads where an allocation would
+ * synchronise the device, hosts with a device-memory budget fixed at
+ * start-up).  trw_walk allocates the kernel's per-warp alias tables on
+ * demand; this entry point keeps them in a fixed 16 MiB device array that
+ * every GPU loading the library holds until exit, so graphs whose maximum
+ * degree exceeds 65535 are rejected with TRW_ERR_CAPACITY.  Arguments and
+ * results are those of trw_walk, except that every non-NULL pointer must be
+ * device memory (staging host buffers would allocate; host pointers give
+ * TRW_ERR_INVALID) and the call is always asynchronous on `stream`.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the array: the
+ * call clears the work-queue head and step counter it keeps there, and
+ * calls that overlap on the GPU race on it, so serialise them (one stream,
+ * or events). */
+int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources,
+                                   int64_t num_walkers, int64_t id_base, int32_t *paths, int32_t path_cap,
+                                   int32_t *lengths, int32_t *counts, uint64_t *steps, trw_stream_t stream);
+
 /* ---- errors ----------------------------------------------------------- */
 
 /* Message of the last failure on the calling thread ("" if none). */

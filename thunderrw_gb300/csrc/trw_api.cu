@@ -493,3 +493,119 @@ int trw_device_error(trw_graph *g, int32_t *code) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Dynamic-alias walks that allocate nothing.
+//
+// Some callers cannot call cudaMalloc when they walk: code running inside a
+// framework that owns all device memory through its own pool and forbids
+// other allocators, latency-critical serving threads where a
+// cudaMalloc/cudaFree would synchronise the whole device, and hosts with a
+// device-memory budget fixed at start-up.  trw_walk allocates the per-warp
+// alias tables of the dynamic-alias kernel on demand; this entry point runs
+// the same kernel with those tables in the fixed array below instead.
+//
+// The array is a file-scope device variable: every GPU that loads this
+// library holds kNoAllocScratchBytes of it until the process exits.  Its
+// first 256 bytes hold the call's work-queue head and step counter (cleared
+// by every call); the rest holds one raw + one table row of max_degree alias
+// slots per warp.  Host code only ever sees a host-side stand-in for the
+// symbol, so the device address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) and cached.
+// ---------------------------------------------------------------------------
+
+static constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB per GPU
+static constexpr size_t kNoAllocStateBytes = 256;          // queue head + step counter
+static __device__ __align__(256) unsigned char trw_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_base[kNoAllocMaxDevices];
+
+// Device address of trw_noalloc_scratch on `device` (which must be current).
+int noalloc_scratch_base(int device, unsigned char **out) {
+    if (device < 0 || device >= kNoAllocMaxDevices) return fail(TRW_ERR_INVALID, "device %d out of range", device);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[device]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, trw_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(TRW_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+        g_noalloc_base[device] = static_cast<unsigned char *>(ptr);
+    }
+    *out = g_noalloc_base[device];
+    return TRW_OK;
+}
+
+}  // namespace
+
+extern "C" int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources,
+                                              int64_t num_walkers, int64_t id_base, int32_t *paths,
+                                              int32_t path_cap, int32_t *lengths, int32_t *counts,
+                                              uint64_t *steps, trw_stream_t stream) {
+    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
+    if (desc->mode != TRW_MODE_DYNAMIC || desc->sampler != TRW_SAMPLER_ALIAS)
+        return fail(TRW_ERR_UNSUPPORTED, "the no-alloc entry point runs dynamic-mode alias sampling only");
+    if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
+    if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
+    const void *ptrs[] = {sources, paths, lengths, counts, steps};
+    for (const void *q : ptrs)
+        if (q && !is_device_ptr(q))
+            return fail(TRW_ERR_INVALID, "the no-alloc entry point takes device pointers only (staging would allocate)");
+    Plan pl;
+    int rc = make_plan(g, desc, pl);
+    if (rc) return rc;
+    const int64_t stride = 2 * (int64_t)std::max(1, g->max_degree);
+    const int64_t table_bytes = (int64_t)(kNoAllocScratchBytes - kNoAllocStateBytes);
+    int64_t warps = table_bytes / ((int64_t)sizeof(AliasSlot) * stride) / 8 * 8;
+    if (warps < 8)
+        return fail(TRW_ERR_CAPACITY, "max degree %d needs %lld bytes of alias scratch for one CTA; the no-alloc scratch "
+                    "holds %lld bytes (max degree <= %lld)", g->max_degree,
+                    (long long)(8 * stride * (int64_t)sizeof(AliasSlot)), (long long)table_bytes,
+                    (long long)(table_bytes / (8 * 2 * (int64_t)sizeof(AliasSlot))));
+    TRW_CUDA(cudaSetDevice(g->device));
+    unsigned char *base = nullptr;
+    rc = noalloc_scratch_base(g->device, &base);
+    if (rc) return rc;
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long *state = reinterpret_cast<unsigned long long *>(base);
+    TRW_CUDA(cudaMemsetAsync(state, 0, 2 * sizeof(unsigned long long), st));
+
+    WalkParams p;
+    std::memset(&p, 0, sizeof p);
+    p.g = dev_view(g);
+    p.length = desc->length;
+    p.schema_len = desc->app == TRW_APP_METAPATH ? desc->schema_len : 1;
+    if (desc->app == TRW_APP_METAPATH)
+        for (int i = 0; i < desc->schema_len; ++i) p.schema[i] = desc->schema[i];
+    p.p_w = desc->p != 0.0 ? 1.0 / desc->p : 0.0;
+    p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
+    p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
+    p.tp = desc->tp;
+    p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
+                 : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
+    p.seed = desc->seed;
+    p.sources = sources;
+    p.num_walkers = num_walkers;
+    p.id_base = id_base;
+    p.paths = paths;
+    p.path_cap = paths ? path_cap : 0;
+    p.lengths = lengths;
+    p.counts = counts;
+    p.queue_head = state;
+    p.steps = state + 1;
+    p.error = g->error;
+    p.alias_scratch = reinterpret_cast<AliasSlot *>(base + kNoAllocStateBytes);
+    p.alias_scratch_stride = stride;
+
+    LaunchShape shape = g->shape[kAlias];
+    shape.engine = kEnginePersistent;
+    shape.num_sms = g->num_sms;
+    shape.max_warps = std::min(warps, warp_engine_warps(p, shape));
+    const cudaError_t le = launch_walk_warp(p, kAlias, pl.update, pl.weight_kind, shape, st);
+    if (le != cudaSuccess) return fail(TRW_ERR_CUDA, "walk launch: %s", cudaGetErrorString(le));
+    if (steps) TRW_CUDA(cudaMemcpyAsync(steps, state + 1, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+    return TRW_OK;
+}
