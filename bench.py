@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--dense", action="store_true", help="PPR: dense Q x N count output instead of sparse CSR")
     return ap.parse_args()
 
 
@@ -257,18 +258,38 @@ def run_ours(args):
     L = N.load()
     import ctypes
 
+    sparse = args.workload == "ppr" and not args.dense
+    out_bytes = 0
     if args.workload == "ppr":
         Q = inp["sources"].numel()
         per_q = inp["per_query"]
-        counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
         steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         src = inp["sources"]
+        if sparse:
+            # size the CSR output from one untimed batch (same shape, other seed)
+            probe = E.ppr_batch_sparse(graph, src, per_q, tp=wl["tp"], seed=999)
+            cap = int(int(probe.offsets[-1].item()) * 1.25) + 1024
+            del probe
+            offsets = torch.empty(Q + 1, dtype=torch.int64, device=dev)
+            vert = torch.empty(cap, dtype=torch.int32, device=dev)
+            vcnt = torch.empty(cap, dtype=torch.int32, device=dev)
+            counts = None
 
-        def one_step(seed, engine="persistent", zero=True):
-            d = E.PPR(wl["tp"]).desc(seed)
-            N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q, per_q,
-                                    ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(steps_dev.data_ptr()),
-                                    1 if zero else 0, N.ENGINES[engine], ctypes.c_void_p(stream.cuda_stream)))
+            def one_step(seed, engine="persistent"):
+                d = E.PPR(wl["tp"]).desc(seed)
+                N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q,
+                                               per_q, ctypes.c_void_p(offsets.data_ptr()),
+                                               ctypes.c_void_p(vert.data_ptr()), ctypes.c_void_p(vcnt.data_ptr()), cap,
+                                               ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
+                                               ctypes.c_void_p(stream.cuda_stream)))
+        else:
+            counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
+
+            def one_step(seed, engine="persistent"):
+                d = E.PPR(wl["tp"]).desc(seed)
+                N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q, per_q,
+                                        ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(steps_dev.data_ptr()),
+                                        1, N.ENGINES[engine], ctypes.c_void_p(stream.cuda_stream)))
     else:
         src = inp["sources"]
         W = src.numel()
@@ -279,7 +300,7 @@ def run_ours(args):
         counts = None
         graph.build_tables("alias", "edge")
 
-        def one_step(seed, engine="persistent", zero=True):
+        def one_step(seed, engine="persistent"):
             d = E.DeepWalk(Lw).desc(seed)
             N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), W, 0,
                                ctypes.c_void_p(paths.data_ptr()), Lw, ctypes.c_void_p(lengths.data_ptr()), None,
@@ -298,7 +319,6 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    step_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     total_steps = 0
     ev0.record(stream)
     for i in range(args.steps):
@@ -306,19 +326,17 @@ def run_ours(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     t_total = ev0.elapsed_time(ev1) / 1e3
-    # per-launch walk-kernel time (the counts are zeroed before the kernel
-    # starts; these events bracket the walk launch alone)
-    kern_ms = []
+    # per-launch walk-kernel time: the library records CUDA events on the
+    # stream around its walk launch (and after the sparse post-processing)
+    graph.profile(True)
+    kern_ms, post_ms = [], []
     for i in range(args.steps):
-        if counts is not None:
-            counts.zero_()
-        a, b = step_evs[i]
-        a.record(stream)
-        one_step(2000 + i, zero=False)
-        b.record(stream)
-        torch.cuda.synchronize()
-        kern_ms.append(a.elapsed_time(b))
+        one_step(2000 + i)
+        wms, pms = graph.last_timings()
+        kern_ms.append(wms)
+        post_ms.append(pms)
         total_steps += int(steps_dev.item())
+    graph.profile(False)
     clocks = sampler.stop()
     steps_per_batch = total_steps / args.steps
     if world > 1:
@@ -332,28 +350,41 @@ def run_ours(args):
         all_steps = steps_per_batch * args.steps
     value = all_steps / t_total
 
-    # ---- e2e: through the C ABI with host buffers (pinned sources in, steps out)
+    # ---- e2e: through the C ABI with host buffers (pinned sources in, results out)
     h_src = src.cpu().pin_memory()
     h_steps = torch.zeros(1, dtype=torch.int64).pin_memory()
+    if sparse:
+        h_off = torch.empty(Q + 1, dtype=torch.int64).pin_memory()
+        h_vert = torch.empty(cap, dtype=torch.int32).pin_memory()
+        h_vcnt = torch.empty(cap, dtype=torch.int32).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_steps = 0
+    e2e_steps, d2h = 0, 0
     for i in range(args.steps):
-        if args.workload == "ppr":
+        if args.workload == "ppr" and sparse:
+            d = E.PPR(wl["tp"]).desc(3000 + i)
+            N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
+                                           ctypes.c_void_p(h_off.data_ptr()), ctypes.c_void_p(h_vert.data_ptr()),
+                                           ctypes.c_void_p(h_vcnt.data_ptr()), cap, ctypes.c_void_p(h_steps.data_ptr()),
+                                           0, ctypes.c_void_p(stream.cuda_stream)))
+            d2h += 8 * (Q + 1) + 8 * int(h_off[-1].item()) + 8
+        elif args.workload == "ppr":
             d = E.PPR(wl["tp"]).desc(3000 + i)
             N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
                                     ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(h_steps.data_ptr()), 1, 0,
                                     ctypes.c_void_p(stream.cuda_stream)))
+            d2h += 8
         else:
             d = E.DeepWalk(wl["length"]).desc(3000 + i)
             N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
                                ctypes.c_void_p(paths.data_ptr()), wl["length"], ctypes.c_void_p(lengths.data_ptr()),
                                None, ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
+            d2h += 8
         e2e_steps += int(h_steps.item())
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
     e2e = {"value": e2e_steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": int(h_src.numel() * 4),
-           "d2h_bytes_per_step": 8}
+           "d2h_bytes_per_step": int(d2h / max(1, args.steps))}
 
     # ---- plain one-launch-per-query form (the comparison engine)
     plain = None
@@ -362,15 +393,24 @@ def run_ours(args):
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if args.workload == "ppr":
+            # one launch per query, one thread per walker, no refill
             a.record(stream)
             for r in range(reps):
-                counts.zero_()
                 for qi in range(Q):
                     d = E.PPR(wl["tp"]).desc(4000 + r)
-                    N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr() + 4 * qi), 1,
-                                            per_q, ctypes.c_void_p(counts.data_ptr() + 4 * qi * graph.n),
-                                            ctypes.c_void_p(steps_dev.data_ptr()), 0, 1,
-                                            ctypes.c_void_p(stream.cuda_stream)))
+                    qsrc = ctypes.c_void_p(src.data_ptr() + 4 * qi)
+                    if sparse:
+                        N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), qsrc, 1, per_q,
+                                                       ctypes.c_void_p(offsets.data_ptr()),
+                                                       ctypes.c_void_p(vert.data_ptr()),
+                                                       ctypes.c_void_p(vcnt.data_ptr()), cap,
+                                                       ctypes.c_void_p(steps_dev.data_ptr()), 1,
+                                                       ctypes.c_void_p(stream.cuda_stream)))
+                    else:
+                        N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), qsrc, 1, per_q,
+                                                ctypes.c_void_p(counts.data_ptr() + 4 * qi * graph.n),
+                                                ctypes.c_void_p(steps_dev.data_ptr()), 1, 1,
+                                                ctypes.c_void_p(stream.cuda_stream)))
             b.record(stream)
             torch.cuda.synchronize()
         else:
@@ -405,6 +445,7 @@ def run_ours(args):
             traffic = float(m.group(1)) * steps_per_batch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "bytes_per_step": bps, "kernel_ms": kmean * 1e3,
+            "post_ms": statistics.mean(post_ms) if sparse else None,
             "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
 
     cpu = None
@@ -425,8 +466,12 @@ def run_ours(args):
             "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": wl["name"], "n": graph.n, "e": graph.e,
                        "steps_per_batch": steps_per_batch, "engine": "persistent",
+                       "counts": ("dense int32 [Q][N], zeroed every step" if args.workload == "ppr" and not sparse
+                                  else "sparse CSR per query (offsets, vertex, int32 count)")
+                       if args.workload == "ppr" else None,
                        "l2": "inputs larger than L2 (adjacency %.2f GB, counts %.1f GB)" % (
                            graph.e * 4 / 1e9, (counts.numel() * 4 / 1e9) if counts is not None else 0)},
+            "kernel_timing": "walk-kernel CUDA events recorded by the library on the launch stream",
             "gpu_launches": args.steps, "clocks": clocks, "e2e": e2e, "roofline": roof,
             "plain": plain, "vs_plain": (value / plain["value"]) if plain else None, "cpu_baseline": cpu,
         }

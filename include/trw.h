@@ -168,8 +168,24 @@ int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *source
                   int64_t walkers_per_query, int32_t *counts, uint64_t *steps, uint32_t flags,
                   int32_t engine, trw_stream_t stream);
 
-/* Autotuned launch shape of the persistent engine for this graph and
- * sampler: walkers per thread (ring depth) and CTAs per SM.  0 = default. */
+/* Batched PPR with sparse output: the same walks as trw_ppr_batch, but the
+ * visit counts come back as per-query (vertex, count) lists instead of a
+ * dense num_queries x n array.  Query q's entries are
+ * vertices[offsets[q] .. offsets[q+1]) with their counts in counts[...];
+ * only vertices with a non-zero count appear, in a canonical order that
+ * depends on the counts alone (not on scheduling).  offsets has
+ * num_queries + 1 entries; vertices and counts hold `capacity` entries.  If
+ * the batch needs more than `capacity` entries, offsets is still written
+ * (offsets[num_queries] is the size needed), no entry is written, and the
+ * call reports TRW_ERR_CAPACITY (synchronous calls) or device error 4. */
+int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
+                         int64_t walkers_per_query, int64_t *offsets, int32_t *vertices, int32_t *counts,
+                         int64_t capacity, uint64_t *steps, int32_t engine, trw_stream_t stream);
+
+/* Launch shape of the persistent engine for this graph and sampler: walkers
+ * per thread (ring depth 1, 2, 4 or 8) and CTAs per SM.  0 = automatic (ring
+ * 1 for sparse PPR tables or fewer than 4 x SMs x 2048 walkers, else 4; as
+ * many CTAs as fit).  thunderrw_gb300/autotune.py measures and sets them. */
 int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm);
 int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_per_thread,
                          int32_t *ctas_per_sm);
@@ -196,6 +212,14 @@ int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_p
 int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources,
                                    int64_t num_walkers, int64_t id_base, int32_t *paths, int32_t path_cap,
                                    int32_t *lengths, int32_t *counts, uint64_t *steps, trw_stream_t stream);
+
+/* Per-call timing (the GPU counterpart of the reference's walking-time
+ * log, creeper.h:411-415,800-803).  While enabled, every walk call records
+ * CUDA events on its stream around its walk-kernel launch and, for
+ * trw_ppr_batch_sparse, after its post-processing launches; trw_profile_read
+ * waits for the last call and returns the two durations in ms. */
+int trw_profile_enable(trw_graph *g, int32_t enable);
+int trw_profile_read(trw_graph *g, float *walk_ms, float *post_ms);
 
 /* ---- errors ----------------------------------------------------------- */
 

@@ -1,0 +1,97 @@
+"""Sparse per-query PPR counts (trw_ppr_batch_sparse) against the dense
+counts of the oracle and of trw_ppr_batch, and determinism of the output
+order across engines (different schedules)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_util import need_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rmat():
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("rmat", 1 << 13, 16, seed=21)
+    return {k: (v.numpy() if hasattr(v, "numpy") else v) for k, v in g.items()}
+
+
+def _check_against_dense(sp, dense):
+    off = sp.offsets.cpu().numpy()
+    vert = sp.vertices.cpu().numpy()
+    cnt = sp.counts.cpu().numpy()
+    Q = off.size - 1
+    for q in range(Q):
+        v, c = vert[off[q]:off[q + 1]], cnt[off[q]:off[q + 1]]
+        nz = np.nonzero(dense[q])[0]
+        assert v.size == nz.size, q
+        assert np.all(c > 0)
+        order = np.argsort(v)
+        np.testing.assert_array_equal(v[order], nz)
+        np.testing.assert_array_equal(c[order], dense[q][nz])
+
+
+def test_sparse_matches_oracle_and_dense(rmat):
+    torch, E = need_gpu()
+    from thunderrw_gb300 import generators as G
+    qs = G.random_sources(torch.from_numpy(rmat["row"]), 41, seed=3).numpy()
+    og = O.Graph(rmat["row"], rmat["adj"])
+    ref = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=77), qs, per_query=700,
+                 want_counts=True, want_lengths=False)
+    g = E.Graph(rmat["row"], rmat["adj"])
+    try:
+        outs = []
+        for engine in ("persistent", "plain"):
+            sp = E.ppr_batch_sparse(g, qs, 700, tp=0.2, seed=77, engine=engine)
+            assert sp.steps == ref["steps"]
+            _check_against_dense(sp, ref["counts"])
+            outs.append(sp)
+        total = int(outs[0].offsets[-1].item())
+        # the order inside each query is canonical: identical under both schedules
+        assert torch.equal(outs[0].offsets, outs[1].offsets)
+        assert torch.equal(outs[0].vertices[:total], outs[1].vertices[:total])
+        assert torch.equal(outs[0].counts[:total], outs[1].counts[:total])
+        dense, _ = E.ppr_batch(g, qs, 700, tp=0.2, seed=77)
+        _check_against_dense(outs[0], dense.cpu().numpy())
+        assert torch.equal(outs[0].dense(g.n), dense)
+    finally:
+        g.close()
+
+
+def test_sparse_capacity_and_reuse(rmat):
+    """Too small a capacity reports the size needed; the tables are left clean."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+    qs = G.random_sources(torch.from_numpy(rmat["row"]), 9, seed=4)
+    g = E.Graph(rmat["row"], rmat["adj"])
+    try:
+        good = E.ppr_batch_sparse(g, qs, 300, tp=0.25, seed=5)
+        need = int(good.offsets[-1].item())
+        L = N.load()
+        off = np.zeros(10, dtype=np.int64)
+        v = np.zeros(8, dtype=np.int32)
+        c = np.zeros(8, dtype=np.int32)
+        steps = np.zeros(1, dtype=np.uint64)
+        d = E.PPR(0.25).desc(5)
+        src = qs.numpy().astype(np.int32)
+        rc = L.trw_ppr_batch_sparse(g.handle, ctypes.byref(d), src.ctypes.data, 9, 300, off.ctypes.data,
+                                    v.ctypes.data, c.ctypes.data, 8, steps.ctypes.data, 0, None)
+        assert rc == -7 and off[-1] == need
+        again = E.ppr_batch_sparse(g, qs, 300, tp=0.25, seed=5)
+        assert torch.equal(again.offsets, good.offsets)
+        assert torch.equal(again.vertices[:need], good.vertices[:need])
+        assert torch.equal(again.counts[:need], good.counts[:need])
+        # host buffers of the right size through the raw C ABI
+        v = np.zeros(need, dtype=np.int32)
+        c = np.zeros(need, dtype=np.int32)
+        rc = L.trw_ppr_batch_sparse(g.handle, ctypes.byref(d), src.ctypes.data, 9, 300, off.ctypes.data,
+                                    v.ctypes.data, c.ctypes.data, need, steps.ctypes.data, 0, None)
+        assert rc == 0 and int(steps[0]) == good.steps
+        np.testing.assert_array_equal(v, good.vertices[:need].cpu().numpy())
+        np.testing.assert_array_equal(c, good.counts[:need].cpu().numpy())
+    finally:
+        g.close()

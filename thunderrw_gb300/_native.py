@@ -23,7 +23,8 @@ ENGINES = {"persistent": 0, "plain": 1}
 WEIGHTS = {"edge": 0, "unit": 1}
 
 EXPORTS = ["trw_graph_create", "trw_graph_destroy", "trw_graph_info", "trw_tables_build", "trw_tables_download",
-           "trw_walk", "trw_ppr_batch", "trw_set_engine_shape", "trw_get_engine_shape", "trw_last_error",
+           "trw_walk", "trw_ppr_batch", "trw_ppr_batch_sparse", "trw_set_engine_shape", "trw_get_engine_shape",
+           "trw_profile_enable", "trw_profile_read", "trw_last_error",
            "trw_device_error", "trw_version"]
 
 
@@ -60,6 +61,9 @@ def load(path: str = LIB_PATH):
     L.trw_tables_download.argtypes = [P, I32, P, ctypes.c_size_t]
     L.trw_walk.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, I32, P, P, P, I32, P]
     L.trw_ppr_batch.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, P, U32, I32, P]
+    L.trw_ppr_batch_sparse.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, P, P, I64, P, I32, P]
+    L.trw_profile_enable.argtypes = [P, I32]
+    L.trw_profile_read.argtypes = [P, P, P]
     L.trw_set_engine_shape.argtypes = [P, I32, I32, I32]
     L.trw_get_engine_shape.argtypes = [P, I32, P, P]
     L.trw_last_error.restype = ctypes.c_char_p

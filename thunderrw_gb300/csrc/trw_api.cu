@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/trw.h"
+#include "trw.h"
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
@@ -104,6 +104,19 @@ struct trw_graph {
     DevBuf alias_scratch;
     cudaEvent_t scratch_done = nullptr;
     LaunchShape shape[5];
+    // sparse PPR: per-query visit tables (kept all-zero between batches),
+    // per-query distinct-vertex counts and output staging
+    DevBuf ppr_tables;
+    int32_t ppr_bits = 0;
+    int64_t ppr_queries = 0;
+    bool ppr_dirty = false;  // a batch stopped between its walk and its emit
+    // optional per-call timing: events around the walk launch and after the
+    // post-processing launches of the last call
+    bool profile = false;
+    cudaEvent_t ev_walk0 = nullptr, ev_walk1 = nullptr, ev_post1 = nullptr;
+    bool have_post = false;
+    DevBuf ppr_distinct;
+    DevBuf stage_out;
     std::mutex mu;
 };
 
@@ -115,6 +128,7 @@ void destroy_graph(trw_graph *g) {
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
+    for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1}) if (e) cudaEventDestroy(e);
     delete g;
 }
 
@@ -214,7 +228,8 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
              int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
              int32_t *lengths, int32_t *counts, int64_t counts_len, bool zero_counts, uint64_t *steps,
-             int32_t engine, cudaStream_t st) {
+             int32_t engine, cudaStream_t st, int32_t *table = nullptr, int32_t table_bits = 0,
+             bool hold_lock = false) {
     if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
     if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
     if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
@@ -222,7 +237,8 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     Plan pl;
     int rc = make_plan(g, desc, pl);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lock(g->mu);
+    std::unique_lock<std::mutex> lock(g->mu, std::defer_lock);
+    if (!hold_lock) lock.lock();
     TRW_CUDA(cudaSetDevice(g->device));
     if (pl.table_kind >= 0) {
         const int have = pl.sampler == kAlias ? g->alias_kind : pl.sampler == kITS ? g->prefix_kind : g->rmax_kind;
@@ -297,11 +313,25 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     p.queue_head = slot.queue_head;
     p.steps = slot.steps;
     p.error = g->error;
+    p.table = table;
+    p.table_bits = table_bits;
 
     LaunchShape shape = g->shape[pl.sampler];
     shape.engine = engine;
     shape.num_sms = g->num_sms;
+    if (shape.ring == 0) {
+        // Automatic ring depth (launch-shape sweeps on GB300): one walker per
+        // lane when visits go to sparse tables (their insert records cost
+        // registers) or when there are too few walkers to give every lane
+        // several; four otherwise.
+        const int64_t lanes = (int64_t)g->num_sms * 2048;
+        shape.ring = (table || num_walkers < 4 * lanes) ? 1 : 4;
+    }
     cudaError_t le;
+    if (g->profile) {
+        TRW_CUDA(cudaEventRecord(g->ev_walk0, st));
+        g->have_post = false;
+    }
     if (pl.warp_family) {
         if (pl.sampler == kAlias) {
             // one raw + one table row of max_degree slots per warp, at most 1 GiB
@@ -322,6 +352,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
         le = launch_walk_thread(p, pl.sampler, pl.update, pl.weight_kind, shape, st);
     }
     if (le != cudaSuccess) return fail(TRW_ERR_CUDA, "walk launch: %s", cudaGetErrorString(le));
+    if (g->profile) TRW_CUDA(cudaEventRecord(g->ev_walk1, st));
     if (steps) TRW_CUDA(cudaMemcpyAsync(steps, slot.steps, sizeof(uint64_t), h_steps ? cudaMemcpyDeviceToHost
                                                                                       : cudaMemcpyDeviceToDevice, st));
     if (h_paths) TRW_CUDA(cudaMemcpyAsync(paths, d_paths, sizeof(int32_t) * (size_t)num_walkers * path_cap,
@@ -463,13 +494,114 @@ int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *source
                     reinterpret_cast<cudaStream_t>(stream));
 }
 
+int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
+                         int64_t walkers_per_query, int64_t *offsets, int32_t *vertices, int32_t *counts,
+                         int64_t capacity, uint64_t *steps, int32_t engine, trw_stream_t stream) {
+    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
+    if (num_queries < 0 || walkers_per_query <= 0) return fail(TRW_ERR_INVALID, "bad batch shape");
+    if (desc->app != TRW_APP_PPR) return fail(TRW_ERR_INVALID, "trw_ppr_batch_sparse runs the PPR app");
+    if (!offsets || capacity < 0 || (capacity > 0 && (!vertices || !counts)))
+        return fail(TRW_ERR_INVALID, "offsets and (vertices, counts) of `capacity` entries are required");
+    if (!(desc->tp >= 1e-6 && desc->tp <= 1.0)) return fail(TRW_ERR_INVALID, "PPR termination probability must be in [1e-6, 1]");
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    // Table size: 2^bits >= 1.25 x the expected visits of a query (walkers /
+    // tp), which bounds its distinct vertices, and never above 2 x the vertex
+    // count (a query cannot visit more).
+    const double visits = (double)walkers_per_query / desc->tp;
+    int32_t bits = 10;
+    while (bits < 30 && (double)(1ll << bits) < 1.25 * visits) ++bits;
+    while (bits > 10 && (1ll << (bits - 1)) >= 2ll * g->n) --bits;
+    if (num_queries > 0 && (g->ppr_bits != bits || g->ppr_queries < num_queries || g->ppr_dirty)) {
+        const size_t bytes = sizeof(int2) * ((size_t)num_queries << bits);
+        TRW_CUDA(g->ppr_tables.ensure(bytes));
+        TRW_CUDA(cudaMemsetAsync(g->ppr_tables.p, 0, bytes, st));
+        g->ppr_bits = bits;
+        g->ppr_queries = num_queries;
+    }
+    TRW_CUDA(g->ppr_distinct.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(1, num_queries)));
+    int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
+    int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
+
+    // output staging for host buffers
+    const bool h_off = !is_device_ptr(offsets);
+    const bool h_v = vertices && !is_device_ptr(vertices);
+    const bool h_c = counts && !is_device_ptr(counts);
+    const size_t b_off = h_off ? align_up(sizeof(int64_t) * (size_t)(num_queries + 1)) : 0;
+    const size_t b_v = h_v ? align_up(sizeof(int32_t) * (size_t)capacity) : 0;
+    const size_t b_c = h_c ? align_up(sizeof(int32_t) * (size_t)capacity) : 0;
+    if (b_off + b_v + b_c) TRW_CUDA(g->stage_out.ensure(b_off + b_v + b_c + 256));
+    char *ob = static_cast<char *>(g->stage_out.p);
+    int64_t *d_off = h_off ? reinterpret_cast<int64_t *>(ob) : offsets;
+    int32_t *d_v = h_v ? reinterpret_cast<int32_t *>(ob + b_off) : vertices;
+    int32_t *d_c = h_c ? reinterpret_cast<int32_t *>(ob + b_off + b_v) : counts;
+
+    g->ppr_dirty = true;
+    int rc = run_walk(g, desc, sources, num_queries, num_queries * walkers_per_query, walkers_per_query, 0, nullptr,
+                      0, nullptr, nullptr, 0, false, steps, engine, st, tables, bits, /*hold_lock=*/true);
+    if (rc) return rc;
+    TRW_CUDA(launch_ppr_offsets(tables, bits, distinct, num_queries, d_off, st));
+    TRW_CUDA(launch_ppr_emit(tables, bits, num_queries, d_off, d_v, d_c, capacity, g->error, st));
+    g->ppr_dirty = false;
+    if (g->profile) {
+        TRW_CUDA(cudaEventRecord(g->ev_post1, st));
+        g->have_post = true;
+    }
+    if (h_off || h_v || h_c) {
+        TRW_CUDA(cudaStreamSynchronize(st));
+        int64_t total = 0;
+        TRW_CUDA(cudaMemcpy(&total, d_off + num_queries, sizeof(int64_t), cudaMemcpyDeviceToHost));
+        if (h_off) TRW_CUDA(cudaMemcpy(offsets, d_off, sizeof(int64_t) * (size_t)(num_queries + 1), cudaMemcpyDeviceToHost));
+        const size_t ent = (size_t)std::min(total, capacity);
+        if (total <= capacity && ent) {
+            if (h_v) TRW_CUDA(cudaMemcpy(vertices, d_v, sizeof(int32_t) * ent, cudaMemcpyDeviceToHost));
+            if (h_c) TRW_CUDA(cudaMemcpy(counts, d_c, sizeof(int32_t) * ent, cudaMemcpyDeviceToHost));
+        }
+        int err = 0;
+        TRW_CUDA(cudaMemcpy(&err, g->error, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            TRW_CUDA(cudaMemset(g->error, 0, sizeof(int)));
+            if (err & kErrCapacity)
+                return fail(TRW_ERR_CAPACITY, "sparse PPR output needs %lld entries, capacity is %lld",
+                            (long long)total, (long long)capacity);
+            return fail(TRW_ERR_DEVICE, "device error word %d", err);
+        }
+    }
+    return TRW_OK;
+}
+
+int trw_profile_enable(trw_graph *g, int32_t enable) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    for (cudaEvent_t *e : {&g->ev_walk0, &g->ev_walk1, &g->ev_post1})
+        if (!*e) TRW_CUDA(cudaEventCreate(e));
+    g->profile = enable != 0;
+    g->have_post = false;
+    return TRW_OK;
+}
+
+int trw_profile_read(trw_graph *g, float *walk_ms, float *post_ms) {
+    if (!g || !g->profile) return fail(TRW_ERR_INVALID, "profiling is not enabled on this graph");
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    TRW_CUDA(cudaEventSynchronize(g->have_post ? g->ev_post1 : g->ev_walk1));
+    float a = 0.f, b = 0.f;
+    TRW_CUDA(cudaEventElapsedTime(&a, g->ev_walk0, g->ev_walk1));
+    if (g->have_post) TRW_CUDA(cudaEventElapsedTime(&b, g->ev_walk1, g->ev_post1));
+    if (walk_ms) *walk_ms = a;
+    if (post_ms) *post_ms = b;
+    return TRW_OK;
+}
+
 int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm) {
     if (!g || sampler < 0 || sampler > 4) return fail(TRW_ERR_INVALID, "bad arguments");
     if (walkers_per_thread != 0 && walkers_per_thread != 1 && walkers_per_thread != 2 && walkers_per_thread != 4 &&
         walkers_per_thread != 8)
         return fail(TRW_ERR_INVALID, "walkers per thread must be 1, 2, 4 or 8");
     std::lock_guard<std::mutex> lock(g->mu);
-    g->shape[sampler].ring = walkers_per_thread ? walkers_per_thread : 4;
+    g->shape[sampler].ring = walkers_per_thread;  // 0 = automatic
     g->shape[sampler].ctas_per_sm = ctas_per_sm > 0 ? ctas_per_sm : 0;
     return TRW_OK;
 }

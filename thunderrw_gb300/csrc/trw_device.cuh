@@ -88,7 +88,7 @@ enum WeightKind : int { kEdgeWeight = 0, kUnitWeight = 1, kNode2Vec = 2, kLabelS
 constexpr int kMaxSchema = 64;
 constexpr uint32_t kMaxTrials = 1u << 20;
 
-enum DeviceError : int { kErrTrials = 1, kErrVertex = 2 };
+enum DeviceError : int { kErrTrials = 1, kErrVertex = 2, kErrCapacity = 4 };
 
 struct WalkParams {
     DevGraph g;
@@ -116,7 +116,49 @@ struct WalkParams {
     // dynamic alias scratch: one table of max_degree slots per warp
     AliasSlot *alias_scratch;
     int64_t alias_scratch_stride;
+    // sparse visit counts: per query an open-addressing table of 2^table_bits
+    // slots stored as 2^table_bits keys (vertex + 1, 0 = empty) followed by
+    // 2^table_bits counts.  Keys and counts live in separate sectors so that
+    // reading a hot key never queues behind the atomic adds to its count.
+    int32_t *table;
+    int32_t table_bits;
 };
+
+// Adds `inc` visits of vertex v to a query's table t (keys t[0..C), counts
+// t[C..2C)): linear probing on key v + 1, 0 = empty.  Which slots end up occupied does not depend on
+// the insertion order; only the order of keys inside a run of occupied
+// slots does.
+__device__ __forceinline__ void table_add(int32_t *t, int32_t bits, int32_t v, int inc, int *error) {
+    const uint32_t mask = (1u << bits) - 1u;
+    uint32_t h = ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
+    const int32_t key = v + 1;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        int k = __ldcg(t + h);
+        if (k == 0) {
+            const int old = atomicCAS(t + h, 0, key);
+            k = old == 0 ? key : old;
+        }
+        if (k == key) { atomicAdd(t + mask + 1 + h, inc); return; }
+        h = (h + 1) & mask;
+    }
+    atomicOr(error, kErrCapacity);  // table full: every slot holds another vertex
+}
+
+// Records a move to `v` for walker query q (dense counts or the sparse
+// table).  Lanes of the warp that record the same (query, vertex) at the same
+// time are merged first (walkers of one query leave the same vertices
+// together), so each distinct pair costs one memory update per warp.
+__device__ __forceinline__ void record_visit(const WalkParams &p, int64_t q, int32_t v) {
+    if (!p.table && !p.counts) return;
+    const unsigned active = __activemask();
+    const unsigned long long key = ((unsigned long long)q << 32) | (uint32_t)v;
+    const unsigned peers = __match_any_sync(active, key);
+    if ((threadIdx.x & 31) != __ffs(peers) - 1) return;
+    const int inc = __popc(peers);
+    if (p.table)
+        table_add(p.table + (q << (p.table_bits + 1)), p.table_bits, v, inc, p.error);
+    else atomicAdd(p.counts + q * (int64_t)p.g.n + v, inc);
+}
 
 // Graph::is_neighbor (graph.h:180-199): binary search for the higher-degree
 // endpoint in the lower-degree endpoint's sorted list (ties search u in v's).

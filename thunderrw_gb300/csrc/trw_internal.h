@@ -15,7 +15,7 @@ constexpr int kEnginePlain = 1;
 
 struct LaunchShape {
     int engine = kEnginePersistent;
-    int ring = 4;         // walkers in flight per lane (thread family)
+    int ring = 0;         // walkers in flight per lane (thread family); 0 = automatic
     int ctas_per_sm = 0;  // 0 = as many as fit
     int num_sms = 1;
     int64_t max_warps = 0;  // dynamic alias: warps with a scratch table
@@ -27,6 +27,11 @@ cudaError_t launch_walk_warp(const WalkParams &p, int sampler, int update, int w
                              const LaunchShape &shape, cudaStream_t st);
 // number of per-warp dynamic-alias scratch tables the warp engine will use
 int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
+
+cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
+                               cudaStream_t st);
+cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets, int32_t *vout,
+                            int32_t *cout, int64_t capacity, int *error, cudaStream_t st);
 
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);

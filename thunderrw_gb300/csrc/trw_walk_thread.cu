@@ -24,7 +24,7 @@ constexpr unsigned kFull = 0xffffffffu;
 
 struct Slot {
     int64_t widx;   // walker index in the call, -1 = empty
-    int64_t cbase;  // visit-count row offset (query * n)
+    int64_t q;      // query of the walker (visit counts)
     int32_t cur, prev, len;
     int2 crow, prow;  // row pairs of cur and prev
 };
@@ -44,7 +44,7 @@ __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx)
     if (p.per_query > 0) { q = idx / p.per_query; src = __ldg(p.sources + q); }
     else src = __ldg(p.sources + idx);
     s.widx = idx;
-    s.cbase = q * (int64_t)p.g.n;
+    s.q = q;
     s.len = 1;
     s.prev = -1;
     s.prow = make_int2(0, 0);
@@ -67,9 +67,87 @@ __device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
     return s;
 }
 
-// One step for each of the R slots, stage by stage.
-template <int S, int U, int WK, int R>
-__device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uint64_t &steps) {
+// A sparse visit-count insert in flight (kSparse kernels), advanced once per
+// ring round so that no round trip stalls the warp:
+//  * recording a visit (end of round i) issues an L2 load of the key in the
+//    vertex's home slot;
+//  * at round i+1, right after the row-pair loads are issued, the load result
+//    is consumed: our key -> add the count (fire-and-forget); empty -> claim
+//    it with a CAS and add the count speculatively; another key -> load the
+//    next slot (linear probing, as table_add);
+//  * the CAS result is consumed when the slot records its next visit, a whole
+//    dependent-load chain later: only a lost race to another key matters; it
+//    takes the speculative count back and probes on.  (Each query's number of
+//    distinct vertices is counted from its table after the walk.)
+struct PendingInsert {
+    int32_t q;      // query of the table, -1 = nothing pending
+    uint32_t h;     // slot being examined
+    uint32_t probes;
+    int32_t key;    // vertex + 1
+    int32_t inc;    // visits merged by the warp
+    int32_t old;    // key found in slot h (by the load or the CAS)
+    int32_t cas;    // 1: `old` came from a CAS of slot h whose count was already added
+};
+
+// Each ring slot alternates between two insert records, so a record is
+// reused two visits after it was filled and its CAS result has long arrived.
+constexpr int kInsertDepth = 2;
+
+__device__ __forceinline__ int32_t *table_of(const WalkParams &p, int32_t q) {
+    return p.table + ((int64_t)q << (p.table_bits + 1));
+}
+
+// Advances the insert by one stage; with `blocking` it runs to completion.
+__device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, bool blocking) {
+    if (pi.q < 0) return;
+    const uint32_t mask = (1u << p.table_bits) - 1u;
+    int32_t *t = table_of(p, pi.q);
+    for (;;) {
+        if (pi.cas) {
+            if (pi.old == 0 || pi.old == pi.key) { pi.q = -1; return; }  // the slot holds our key
+            atomicAdd(t + mask + 1 + pi.h, -pi.inc);                       // lost it to another vertex
+        } else {
+            if (pi.old == pi.key) {
+                atomicAdd(t + mask + 1 + pi.h, pi.inc);
+                pi.q = -1;
+                return;
+            }
+            if (pi.old == 0) {
+                pi.old = atomicCAS(t + pi.h, 0, pi.key);
+                atomicAdd(t + mask + 1 + pi.h, pi.inc);
+                pi.cas = 1;
+                if (!blocking) return;
+                continue;
+            }
+        }
+        if (++pi.probes > mask) {  // every slot holds another vertex
+            atomicOr(p.error, kErrCapacity);
+            pi.q = -1;
+            return;
+        }
+        pi.h = (pi.h + 1) & mask;
+        pi.old = __ldcg(t + pi.h);
+        pi.cas = 0;
+        if (!blocking) return;
+    }
+}
+
+__device__ __forceinline__ void start_insert(const WalkParams &p, PendingInsert &pi, int64_t q, int32_t v, int inc) {
+    if (pi.q >= 0) resolve(p, pi, true);  // filled two visits ago: normally already settled
+    pi.q = (int32_t)q;
+    pi.h = ((uint32_t)v * 0x9E3779B1u) >> (32 - p.table_bits);
+    pi.probes = 0;
+    pi.key = v + 1;
+    pi.inc = inc;
+    pi.old = __ldcg(table_of(p, pi.q) + pi.h);
+    pi.cas = 0;
+}
+
+// One step for each of the R slots, stage by stage.  kSparse: visits go to
+// the per-query tables through the pipelined inserts in `pend`.
+template <int S, int U, int WK, int R, bool kSparse>
+__device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uint64_t &steps,
+                                          PendingInsert (&pend)[R][kInsertDepth], uint32_t &flip) {
     const DevGraph &g = p.g;
     int32_t nxt[R];
     bool moved[R];
@@ -79,6 +157,13 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         moved[r] = false;
         nxt[r] = 0;
         if (s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
+    }
+    if (kSparse) {  // while the row pairs are in flight
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < kInsertDepth; ++k)
+                if (pend[r][k].q >= 0 && !pend[r][k].cas) resolve(p, pend[r][k], false);
     }
 #pragma unroll
     for (int r = 0; r < R; ++r)
@@ -206,7 +291,17 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
         s[r].len += 1;
         steps += 1;
-        if (p.counts) atomicAdd(p.counts + s[r].cbase + nxt[r], 1);
+        if (kSparse) {
+            const unsigned peers = __match_any_sync(__activemask(), ((unsigned long long)s[r].q << 32) | (uint32_t)nxt[r]);
+            if ((threadIdx.x & 31) == __ffs(peers) - 1) {
+                // constant indices keep the records in registers
+                if ((flip >> r) & 1u) start_insert(p, pend[r][1], s[r].q, nxt[r], __popc(peers));
+                else start_insert(p, pend[r][0], s[r].q, nxt[r], __popc(peers));
+                flip ^= 1u << r;
+            }
+        } else {
+            record_visit(p, s[r].q, nxt[r]);
+        }
         if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) finish(p, s[r]);
     }
 }
@@ -218,13 +313,19 @@ __device__ __forceinline__ void flush_steps(const WalkParams &p, uint64_t steps)
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.steps, v);
 }
 
-template <int S, int U, int WK, int R>
+template <int S, int U, int WK, int R, bool kSparse>
 __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams p) {
     const int lane = threadIdx.x & 31;
     constexpr unsigned long long kChunk = 32ull * R * 2;
     Slot s[R];
+    PendingInsert pend[R][kInsertDepth];
+    uint32_t flip = 0;
 #pragma unroll
-    for (int r = 0; r < R; ++r) s[r].widx = -1;
+    for (int r = 0; r < R; ++r) {
+        s[r].widx = -1;
+#pragma unroll
+        for (int k = 0; k < kInsertDepth; ++k) pend[r][k].q = -1;
+    }
     uint64_t steps = 0;
     unsigned long long res_next = 0, res_end = 0;
     bool drained = false;
@@ -253,19 +354,30 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
 #pragma unroll
         for (int r = 0; r < R; ++r) live |= s[r].widx >= 0;
         if (!__any_sync(kFull, live)) break;
-        step_ring<S, U, WK, R>(p, s, steps);
+        step_ring<S, U, WK, R, kSparse>(p, s, steps, pend, flip);
+    }
+    if (kSparse) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[r][k], true);
     }
     flush_steps(p, steps);
 }
 
-template <int S, int U, int WK>
+template <int S, int U, int WK, bool kSparse>
 __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t steps = 0;
     if (idx < p.num_walkers) {
         Slot s[1];
+        PendingInsert pend[1][kInsertDepth];
+        uint32_t flip = 0;
+        for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
         admit(p, s[0], idx);
-        while (s[0].widx >= 0) step_ring<S, U, WK, 1>(p, s, steps);
+        while (s[0].widx >= 0) step_ring<S, U, WK, 1, kSparse>(p, s, steps, pend, flip);
+        if (kSparse)
+            for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[0][k], true);
     }
     flush_steps(p, steps);
 }
@@ -277,32 +389,39 @@ int max_occupancy(K kernel) {
     return n;
 }
 
-template <int S, int U, int WK, int R>
+template <int S, int U, int WK, int R, bool kSparse>
 cudaError_t launch_persistent(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
-    static const int max_occ = max_occupancy(walk_persistent<S, U, WK, R>);
+    static const int max_occ = max_occupancy(walk_persistent<S, U, WK, R, kSparse>);
     const int per_sm = shape.ctas_per_sm > 0 ? min(shape.ctas_per_sm, max_occ) : max_occ;
     int64_t grid = (int64_t)shape.num_sms * per_sm;
     const int64_t useful = (p.num_walkers + (int64_t)kThreadBlock * R - 1) / ((int64_t)kThreadBlock * R);
     if (useful < grid) grid = useful;
     if (grid <= 0) return cudaSuccess;
-    walk_persistent<S, U, WK, R><<<(unsigned)grid, kThreadBlock, 0, st>>>(p);
+    walk_persistent<S, U, WK, R, kSparse><<<(unsigned)grid, kThreadBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
-template <int S, int U, int WK>
-cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
+template <int S, int U, int WK, bool kSparse>
+cudaError_t launch_mode(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
     if (shape.engine == kEnginePlain) {
         const int64_t blocks = (p.num_walkers + kThreadBlock - 1) / kThreadBlock;
         if (blocks <= 0) return cudaSuccess;
-        walk_plain<S, U, WK><<<(unsigned)blocks, kThreadBlock, 0, st>>>(p);
+        walk_plain<S, U, WK, kSparse><<<(unsigned)blocks, kThreadBlock, 0, st>>>(p);
         return cudaGetLastError();
     }
     switch (shape.ring) {
-    case 1: return launch_persistent<S, U, WK, 1>(p, shape, st);
-    case 2: return launch_persistent<S, U, WK, 2>(p, shape, st);
-    case 8: return launch_persistent<S, U, WK, 8>(p, shape, st);
-    default: return launch_persistent<S, U, WK, 4>(p, shape, st);
+    case 1: return launch_persistent<S, U, WK, 1, kSparse>(p, shape, st);
+    case 2: return launch_persistent<S, U, WK, 2, kSparse>(p, shape, st);
+    case 8: return launch_persistent<S, U, WK, 8, kSparse>(p, shape, st);
+    default: return launch_persistent<S, U, WK, 4, kSparse>(p, shape, st);
     }
+}
+
+// Sparse visit tables only exist for PPR (geometric update).
+template <int S, int U, int WK>
+cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
+    if (U == kGeometric && p.table) return launch_mode<S, U, WK, true>(p, shape, st);
+    return launch_mode<S, U, WK, false>(p, shape, st);
 }
 
 }  // namespace

@@ -29,7 +29,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 
 struct WSlot {
-    int64_t widx, cbase;
+    int64_t widx, q;
     int32_t cur, prev, len;
     int2 crow, prow;
 };
@@ -49,7 +49,7 @@ __device__ __forceinline__ void wadmit(const WalkParams &p, WSlot &s, int64_t id
     if (p.per_query > 0) { q = idx / p.per_query; src = __ldg(p.sources + q); }
     else src = __ldg(p.sources + idx);
     s.widx = idx;
-    s.cbase = q * (int64_t)p.g.n;
+    s.q = q;
     s.len = 1;
     s.prev = -1;
     s.prow = make_int2(0, 0);
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_warp(const WalkParams p, in
                 if (p.paths && s.len < p.path_cap) p.paths[s.widx * (int64_t)p.path_cap + s.len] = my_nxt;
                 s.len += 1;
                 steps += 1;
-                if (p.counts) atomicAdd(p.counts + s.cbase + my_nxt, 1);
+                record_visit(p, s.q, my_nxt);
                 if (app_update<U>(p, (uint64_t)(p.id_base + s.widx), s.len)) wfinish(p, s);
             }
         }

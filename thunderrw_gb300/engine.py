@@ -175,6 +175,15 @@ class Graph:
         N.check(_lib().trw_get_engine_shape(self._h, N.SAMPLERS[sampler], ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def profile(self, enable: bool = True):
+        N.check(_lib().trw_profile_enable(self._h, 1 if enable else 0))
+
+    def last_timings(self):
+        """(walk kernel ms, post-processing ms) of the last walk call (profiling on)."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        N.check(_lib().trw_profile_read(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def device_error(self) -> int:
         c = ctypes.c_int32()
         N.check(_lib().trw_device_error(self._h, ctypes.byref(c)))
@@ -252,3 +261,56 @@ def ppr_batch(graph: Graph, sources, walkers_per_query: int, tp: float = 0.2, se
                                  _ptr(steps), 1 if zero_counts else 0, N.ENGINES[engine],
                                  ctypes.c_void_p(_stream_ptr(stream))))
     return counts, steps
+
+
+@dataclass
+class SparseCounts:
+    """Per-query visit counts in CSR form: query q's vertices are
+    ``vertices[offsets[q]:offsets[q+1]]`` with ``counts`` alongside."""
+    offsets: torch.Tensor
+    vertices: torch.Tensor
+    counts: torch.Tensor
+    steps_dev: torch.Tensor = field(repr=False)
+
+    @property
+    def steps(self) -> int:
+        return int(self.steps_dev.item())
+
+    def dense(self, n: int) -> torch.Tensor:
+        q = self.offsets.numel() - 1
+        out = torch.zeros((q, n), dtype=torch.int32, device=self.vertices.device)
+        total = int(self.offsets[-1].item())
+        rows = torch.repeat_interleave(torch.arange(q, device=self.vertices.device),
+                                       (self.offsets[1:] - self.offsets[:-1]))
+        out[rows, self.vertices[:total].long()] = self.counts[:total]
+        return out
+
+
+def ppr_batch_sparse(graph: Graph, sources, walkers_per_query: int, tp: float = 0.2, seed: int = 1,
+                     capacity: Optional[int] = None, engine: str = "persistent", stream=None,
+                     out: Optional[SparseCounts] = None) -> SparseCounts:
+    """Batched PPR with sparse per-query (vertex, count) output
+    (trw_ppr_batch_sparse).  If the output does not fit ``capacity`` entries,
+    the batch is rerun with the exact size (results are identical)."""
+    dev = graph.device
+    src = _dev(sources, torch.int32, dev)
+    Q = src.numel()
+    if out is None:
+        if capacity is None:
+            capacity = Q * min(graph.n, max(1, int(walkers_per_query * 3)))
+        out = SparseCounts(torch.empty(Q + 1, dtype=torch.int64, device=dev),
+                           torch.empty(max(1, capacity), dtype=torch.int32, device=dev),
+                           torch.empty(max(1, capacity), dtype=torch.int32, device=dev),
+                           torch.zeros(1, dtype=torch.int64, device=dev))
+    cap = out.vertices.numel()
+    d = PPR(tp).desc(seed)
+    N.check(_lib().trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), _ptr(src), Q, int(walkers_per_query),
+                                        _ptr(out.offsets), _ptr(out.vertices), _ptr(out.counts), cap,
+                                        _ptr(out.steps_dev), N.ENGINES[engine], ctypes.c_void_p(_stream_ptr(stream))))
+    total = int(out.offsets[-1].item())
+    if total > cap:
+        graph.device_error()  # clears the capacity flag of the first attempt
+        out = SparseCounts(out.offsets, torch.empty(total, dtype=torch.int32, device=dev),
+                           torch.empty(total, dtype=torch.int32, device=dev), out.steps_dev)
+        return ppr_batch_sparse(graph, src, walkers_per_query, tp, seed, engine=engine, stream=stream, out=out)
+    return out
