@@ -520,7 +520,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         g->ppr_bits = bits;
         g->ppr_queries = num_queries;
     }
-    TRW_CUDA(g->ppr_distinct.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(1, num_queries)));
+    TRW_CUDA(g->ppr_distinct.ensure(sizeof(int32_t) * 17 * (size_t)std::max<int64_t>(1, num_queries)));
     int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
     int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
 
@@ -542,7 +542,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
                       0, nullptr, nullptr, 0, false, steps, engine, st, tables, bits, /*hold_lock=*/true);
     if (rc) return rc;
     TRW_CUDA(launch_ppr_offsets(tables, bits, distinct, num_queries, d_off, st));
-    TRW_CUDA(launch_ppr_emit(tables, bits, num_queries, d_off, d_v, d_c, capacity, g->error, st));
+    TRW_CUDA(launch_ppr_emit(tables, bits, num_queries, d_off, distinct, d_v, d_c, capacity, g->error, st));
     g->ppr_dirty = false;
     if (g->profile) {
         TRW_CUDA(cudaEventRecord(g->ev_post1, st));

@@ -4,9 +4,11 @@
 // arithmetic (static_initialization, creeper.h:102-175; the offline
 // alias_preprocess.cpp:30-73, its_preprocess.cpp:21-34,
 // rejection_preprocess.cpp:24-27).  Bit-identical tables need the same
-// operation order, so every vertex's arithmetic chain stays sequential in one
-// thread; the parallelism is across vertices.  The maximum is
-// order-independent and uses the same per-vertex loop for simplicity.
+// operation order, so every vertex's arithmetic chain stays sequential.
+// Rows of up to kWarpRow entries are built one thread per vertex; longer rows
+// (the hubs of power-law graphs) one warp per vertex, where the warp loads
+// 32 entries at a time with coalesced loads and runs the sequential chains in
+// lockstep through shuffles.  The maximum is order-independent.
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
@@ -28,12 +30,14 @@ __device__ __forceinline__ double sweight(const DevGraph &g, int unit, int64_t e
 // slots j+1.. in the same order.  Slot j therefore holds P[j] (in .first)
 // until it is written; a large that turns small parks its final value in its
 // own slot, which is written exactly when it is popped.
+constexpr int32_t kWarpRow = 32;
+
 __global__ void build_alias_kernel(const DevGraph g, int unit, AliasSlot *out) {
     const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.n) return;
     const int2 r = __ldg(g.rows + v);
     const int32_t d = r.y - r.x;
-    if (d <= 0) return;
+    if (d <= 0 || d > kWarpRow) return;
     const int32_t *nb = g.adj + r.x;
     AliasSlot *tab = out + r.x;
     double sum = 0.0;
@@ -84,12 +88,145 @@ __global__ void build_prefix_kernel(const DevGraph g, int unit, double *out) {
     const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.n) return;
     const int2 r = __ldg(g.rows + v);
-    if (r.y <= r.x) return;
+    if (r.y <= r.x || r.y - r.x > kWarpRow) return;
     double acc = sweight(g, unit, r.x);
     out[r.x] = acc;
     for (int32_t i = r.x + 1; i < r.y; ++i) {
         acc = acc + sweight(g, unit, i);
         out[i] = acc;
+    }
+}
+
+// ---- one warp per long row -------------------------------------------------
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Left fold of the row's weights (std::accumulate order): every lane keeps
+// the same running sum, adding the 32 staged entries in order.
+__device__ __forceinline__ double warp_row_sum(const DevGraph &g, int unit, int2 r) {
+    const int lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (int32_t base = r.x; base < r.y; base += 32) {
+        const int32_t i = base + lane;
+        const double w = i < r.y ? sweight(g, unit, i) : 0.0;
+        const int m = min(32, r.y - base);
+        for (int k = 0; k < m; ++k) acc = acc + __shfl_sync(kFull, w, k);
+    }
+    return acc;
+}
+
+// its_initialization for a long row: the same left-to-right chain; lane k
+// keeps the value after adding entry k of the block and stores it (coalesced).
+__global__ void build_prefix_warp_kernel(const DevGraph g, int unit, double *out) {
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (v >= g.n) return;
+    const int2 r = __ldg(g.rows + v);
+    if (r.y - r.x <= kWarpRow) return;
+    double acc = 0.0;
+    bool first = true;
+    for (int32_t base = r.x; base < r.y; base += 32) {
+        const int32_t i = base + lane;
+        const double w = i < r.y ? sweight(g, unit, i) : 0.0;
+        const int m = min(32, r.y - base);
+        double mine = 0.0;
+        for (int k = 0; k < m; ++k) {
+            const double x = __shfl_sync(kFull, w, k);
+            acc = first ? x : acc + x;  // dst[0] = src[0]; dst[i] = dst[i-1] + src[i]
+            first = false;
+            if (lane == k) mine = acc;
+        }
+        if (i < r.y) out[i] = mine;
+    }
+}
+
+// alias_initialization for a long row (same slot formulation as the thread
+// kernel above): ballot-based stable partition, then the pairing loop run in
+// lockstep by the warp with 32-entry register blocks of the small queue and
+// of the large list; table entries hold neighbour indices until a final
+// parallel pass maps them to vertex ids.
+__global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *out) {
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (v >= g.n) return;
+    const int2 r = __ldg(g.rows + v);
+    const int32_t d = r.y - r.x;
+    if (d <= kWarpRow) return;
+    const int32_t *nb = g.adj + r.x;
+    AliasSlot *tab = out + r.x;
+    const double avg = warp_row_sum(g, unit, r) / d;
+    if (avg == 0.0) {
+        for (int32_t j = lane; j < d; j += 32) { const int32_t x = __ldg(nb + j); tab[j] = {1.0, x, x}; }
+        return;
+    }
+    // stable partition: smalls (w/avg < 1) first, in index order
+    int32_t ns = 0;
+    for (int32_t base = 0; base < d; base += 32) {
+        const int32_t j = base + lane;
+        ns += __popc(__ballot_sync(kFull, j < d && sweight(g, unit, r.x + j) / avg < 1));
+    }
+    int32_t sb = 0, lb = ns;
+    for (int32_t base = 0; base < d; base += 32) {
+        const int32_t j = base + lane;
+        const bool in = j < d;
+        const double sc = in ? sweight(g, unit, r.x + j) / avg : 0.0;
+        const unsigned ms = __ballot_sync(kFull, in && sc < 1), ml = __ballot_sync(kFull, in && !(sc < 1));
+        if (in) {
+            const unsigned below = (1u << lane) - 1u;
+            const int32_t pos = sc < 1 ? sb + __popc(ms & below) : lb + __popc(ml & below);
+            tab[pos].prob = sc;
+            tab[pos].first = j;
+        }
+        sb += __popc(ms);
+        lb += __popc(ml);
+    }
+    __syncwarp();
+    // pairing loop (alias_sampling.h:29-39) in lockstep
+    const int32_t nl = d - ns;
+    int32_t sp = 0, c = 0;
+    int32_t sblk = -1, svalid = 0, lblk = -1;
+    double s_prob = 0.0, l_prob = 0.0;
+    int32_t s_idx = 0, l_idx = 0;
+    auto load_l = [&](int32_t pos) {  // large list entries are untouched until stashed
+        lblk = pos;
+        const int32_t j = pos + lane;
+        if (j < d) { l_prob = tab[j].prob; l_idx = tab[j].first; }
+    };
+    if (nl) load_l(ns);
+    double vl = __shfl_sync(kFull, l_prob, 0);
+    while (sp < ns + c && c < nl) {
+        // small queue head: slot sp; slots >= ns hold larges whose final value
+        // was stashed there, so a cached block is only valid below ns + c at load
+        if (sblk < 0 || sp >= sblk + 32 || sp >= svalid) {
+            __syncwarp();
+            sblk = sp;
+            svalid = ns + c;
+            const int32_t j = sp + lane;
+            if (j < d) { s_prob = tab[j].prob; s_idx = tab[j].first; }
+        }
+        const double vs = __shfl_sync(kFull, s_prob, sp - sblk);
+        const int32_t si = __shfl_sync(kFull, s_idx, sp - sblk);
+        const int32_t li = __shfl_sync(kFull, l_idx, ns + c - lblk);
+        if (lane == 0) { tab[sp].prob = vs; tab[sp].first = si; tab[sp].second = li; }
+        ++sp;
+        vl = vl + vs - 1;  // src[large] + src[small] - 1
+        if (vl < 1) {
+            if (lane == 0) tab[ns + c].prob = vl;
+            ++c;
+            if (c < nl) {
+                if (ns + c >= lblk + 32) { __syncwarp(); load_l(ns + c); }
+                vl = __shfl_sync(kFull, l_prob, ns + c - lblk);
+            }
+        }
+    }
+    __syncwarp();
+    // indices -> vertex ids; leftovers (slots >= sp) get probability 1
+    for (int32_t j = lane; j < d; j += 32) {
+        AliasSlot e = tab[j];
+        if (j >= sp) { e.prob = 1.0; e.second = e.first; }
+        e.first = __ldg(nb + e.first);
+        e.second = __ldg(nb + e.second);
+        tab[j] = e;
     }
 }
 
@@ -109,23 +246,37 @@ __global__ void build_max_kernel(const DevGraph g, int unit, double *out) {
 // CSR validation: offsets start at 0, end at e and never decrease; every
 // neighbour id is in range; optionally every row is sorted ascending
 // (Graph::is_sort, graph.cpp:764-776).  Also packs the (begin, end) pairs.
+// One warp per vertex reads the row with coalesced loads; each lane compares
+// its entry with the previous lane's (and the previous chunk's last entry).
 __global__ void validate_kernel(const int64_t *row, const int32_t *adj, int32_t n, int64_t e, int check_sorted,
                                 int2 *rows_out, int *bad, int *max_degree) {
-    const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (v >= n) return;
     const int64_t b = row[v], en = row[v + 1];
-    if (v == 0 && b != 0) atomicOr(bad, 1);
-    if (v == n - 1 && en != e) atomicOr(bad, 1);
-    if (b < 0 || en < b || en > e) { atomicOr(bad, 2); return; }
-    rows_out[v] = make_int2((int32_t)b, (int32_t)en);
-    atomicMax(max_degree, (int)(en - b));
-    int32_t last = -1;
-    for (int64_t i = b; i < en; ++i) {
-        const int32_t x = adj[i];
-        if (x < 0 || x >= n) { atomicOr(bad, 4); return; }
-        if (check_sorted && x < last) { atomicOr(bad, 8); return; }
-        last = x;
+    if (lane == 0) {
+        if (v == 0 && b != 0) atomicOr(bad, 1);
+        if (v == n - 1 && en != e) atomicOr(bad, 1);
     }
+    if (b < 0 || en < b || en > e) { if (lane == 0) atomicOr(bad, 2); return; }
+    if (lane == 0) {
+        rows_out[v] = make_int2((int32_t)b, (int32_t)en);
+        atomicMax(max_degree, (int)(en - b));
+    }
+    int32_t carry = -1;  // last entry of the previous chunk
+    int flags = 0;
+    for (int64_t base = b; base < en; base += 32) {
+        const int64_t i = base + lane;
+        const bool in = i < en;
+        const int32_t x = in ? adj[i] : 0x7fffffff;
+        if (in && (x < 0 || x >= n)) flags |= 4;
+        int32_t left = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane == 0) left = carry;
+        if (check_sorted && in && x < left) flags |= 8;
+        carry = __shfl_sync(0xffffffffu, x, 31);
+    }
+    flags = __reduce_or_sync(0xffffffffu, flags);
+    if (lane == 0 && flags) atomicOr(bad, flags);
 }
 
 inline unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
@@ -135,12 +286,14 @@ inline unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_alias_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    build_alias_warp_kernel<<<blocks_for((int64_t)g.n * 32), 256, 0, st>>>(g, unit, out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_prefix_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    build_prefix_warp_kernel<<<blocks_for((int64_t)g.n * 32), 256, 0, st>>>(g, unit, out);
     return cudaGetLastError();
 }
 
@@ -153,7 +306,7 @@ cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStrea
 cudaError_t launch_validate_graph(const int64_t *row, const int32_t *adj, int32_t n, int64_t e, int check_sorted,
                                   int2 *rows_out, int *bad, int *max_degree, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    validate_kernel<<<blocks_for(n), 256, 0, st>>>(row, adj, n, e, check_sorted, rows_out, bad, max_degree);
+    validate_kernel<<<blocks_for((int64_t)n * 32), 256, 0, st>>>(row, adj, n, e, check_sorted, rows_out, bad, max_degree);
     return cudaGetLastError();
 }
 

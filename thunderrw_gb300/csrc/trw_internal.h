@@ -30,8 +30,10 @@ int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
 
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st);
-cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets, int32_t *vout,
-                            int32_t *cout, int64_t capacity, int *error, cudaStream_t st);
+// `distinct` holds nq totals followed by nq x 16 segment counts
+cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
+                            const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
+                            cudaStream_t st);
 
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);
