@@ -221,6 +221,56 @@ int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc *desc, cons
 int trw_profile_enable(trw_graph *g, int32_t enable);
 int trw_profile_read(trw_graph *g, float *walk_ms, float *post_ms);
 
+/* ---- serving ---------------------------------------------------------- */
+
+/* A request loop over a resident graph (no counterpart in the reference,
+ * which runs one compute() per process).  Requests of any app and size are
+ * admitted in arrival order whenever one of `max_inflight` streams is free and
+ * the request's device memory fits `hbm_budget_bytes` (0 = 80 % of the free
+ * HBM at start); each admitted request runs on its own stream, overlapping the
+ * ones already running.  Results stay in HBM until trw_server_release. */
+typedef struct trw_server trw_server;
+
+typedef struct {
+    trw_walk_desc desc;
+    const int32_t *sources;     /* host memory, copied at submit: num_walkers (walks) or num_queries (PPR) */
+    int64_t num_walkers;        /* walks: walker count */
+    int64_t id_base;            /* walks: Philox id of walker 0 */
+    int32_t path_cap;           /* walks: path entries per walker, 0 = lengths only */
+    int64_t num_queries;        /* sparse PPR batch: number of queries */
+    int64_t walkers_per_query;  /* > 0: the request is trw_ppr_batch_sparse */
+} trw_request;
+
+typedef struct {
+    int32_t state;       /* 0 queued, 1 running, 2 done, 3 failed */
+    double latency_ms;   /* submit -> results complete in HBM */
+    double queue_ms;     /* submit -> launch */
+    uint64_t steps;
+    int64_t entries;     /* sparse PPR: (vertex, count) entries */
+} trw_request_status;
+
+typedef struct {
+    uint64_t submitted, completed, failed, steps;
+    int64_t queued, running;
+    size_t hbm_in_use;
+    double p50_ms, p99_ms, max_ms, elapsed_s;
+} trw_serving_stats;
+
+int trw_server_start(trw_graph *g, size_t hbm_budget_bytes, int32_t max_inflight, trw_server **out);
+/* TRW_ERR_BUSY when the queue is full, TRW_ERR_CAPACITY when the request
+ * alone exceeds the budget. */
+int trw_server_submit(trw_server *s, const trw_request *req, uint64_t *ticket);
+/* Waits up to timeout_ms (< 0: forever) for the request to finish. */
+int trw_server_wait(trw_server *s, uint64_t ticket, int32_t timeout_ms, trw_request_status *status);
+/* Copies a finished request's outputs to host buffers (walks: paths,
+ * lengths; PPR: offsets, and vertices/counts of `capacity` entries). */
+int trw_server_result(trw_server *s, uint64_t ticket, int32_t *paths, int32_t *lengths, int64_t *offsets,
+                      int32_t *vertices, int32_t *counts, int64_t capacity);
+int trw_server_release(trw_server *s, uint64_t ticket);
+int trw_server_stats(trw_server *s, trw_serving_stats *out);
+/* Finishes the queued and running requests, then frees everything. */
+int trw_server_stop(trw_server *s);
+
 /* ---- errors ----------------------------------------------------------- */
 
 /* Message of the last failure on the calling thread ("" if none). */

@@ -110,6 +110,8 @@ struct trw_graph {
     int32_t ppr_bits = 0;
     int64_t ppr_queries = 0;
     bool ppr_dirty = false;  // a batch stopped between its walk and its emit
+    cudaEvent_t ppr_done = nullptr;  // last sparse batch's emit: the tables are free after it
+    cudaEvent_t tables_done = nullptr;  // last static-table build: walks on any stream wait for it
     // optional per-call timing: events around the walk launch and after the
     // post-processing launches of the last call
     bool profile = false;
@@ -128,7 +130,8 @@ void destroy_graph(trw_graph *g) {
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
-    for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
+        if (e) cudaEventDestroy(e);
     delete g;
 }
 
@@ -143,6 +146,10 @@ int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
     const DevGraph d = dev_view(g);
     if (kind == TRW_WEIGHTS_EDGE && !g->weight) return fail(TRW_ERR_INVALID, "edge weights were not supplied");
     const int unit = kind == TRW_WEIGHTS_UNIT;
+    // rebuilding a table in place: let walks still reading it (on any stream) finish
+    if ((sampler == TRW_SAMPLER_ALIAS && g->alias) || (sampler == TRW_SAMPLER_ITS && g->prefix) ||
+        (sampler == TRW_SAMPLER_REJECTION && g->rmax))
+        TRW_CUDA(cudaDeviceSynchronize());
     if (sampler == TRW_SAMPLER_ALIAS) {
         if (!g->alias) TRW_CUDA(cudaMalloc(&g->alias, sizeof(AliasSlot) * (size_t)(g->e ? g->e : 1)));
         TRW_CUDA(launch_build_alias(d, unit, g->alias, st));
@@ -158,6 +165,7 @@ int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
     } else {
         return fail(TRW_ERR_INVALID, "sampler %d has no static table", sampler);
     }
+    TRW_CUDA(cudaEventRecord(g->tables_done, st));
     return TRW_OK;
 }
 
@@ -246,6 +254,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
             rc = build_table(g, pl.sampler, pl.table_kind, st);
             if (rc) return rc;
         }
+        TRW_CUDA(cudaStreamWaitEvent(st, g->tables_done, 0));  // built on another stream, perhaps
     }
 
     // Stage host buffers.
@@ -414,6 +423,8 @@ int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *w
         chk(cudaEventCreateWithFlags(&g->slots[i].done, cudaEventDisableTiming));
     }
     chk(cudaEventCreateWithFlags(&g->scratch_done, cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&g->ppr_done, cudaEventDisableTiming));
+    chk(cudaEventCreateWithFlags(&g->tables_done, cudaEventDisableTiming));
     chk(cudaMemset(g->state, 0, sizeof(unsigned long long) * (2 * kEngineSlots + 1)));
     chk(cudaMemcpy(d_row, row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDefault));
     if (e) chk(cudaMemcpy(g->adj, adj, sizeof(int32_t) * (size_t)e, cudaMemcpyDefault));
@@ -506,6 +517,9 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     std::lock_guard<std::mutex> lock(g->mu);
     TRW_CUDA(cudaSetDevice(g->device));
+    // The tables (and counters) are shared by every sparse batch on this
+    // graph: calls on different streams run one after the other on the device.
+    TRW_CUDA(cudaStreamWaitEvent(st, g->ppr_done, 0));
     // Table size: 2^bits >= 1.25 x the expected visits of a query (walkers /
     // tp), which bounds its distinct vertices, and never above 2 x the vertex
     // count (a query cannot visit more).
@@ -543,6 +557,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     if (rc) return rc;
     TRW_CUDA(launch_ppr_offsets(tables, bits, distinct, num_queries, d_off, st));
     TRW_CUDA(launch_ppr_emit(tables, bits, num_queries, d_off, distinct, d_v, d_c, capacity, g->error, st));
+    TRW_CUDA(cudaEventRecord(g->ppr_done, st));
     g->ppr_dirty = false;
     if (g->profile) {
         TRW_CUDA(cudaEventRecord(g->ev_post1, st));
