@@ -45,6 +45,11 @@ WORKLOADS = {
                      "uniform sampling tp=0.2, int32 visit counts per query"),
     "deepwalk": dict(kind="chunglu", n=1 << 18, deg=16, length=80,
                      name="deepwalk static alias chung-lu(2.1) N=2^18 deg=16, one walker per vertex, L=80"),
+    "node2vec": dict(kind="rmat", n=1 << 24, deg=16, length=80, p=2.0, q=0.5,
+                     name="node2vec p=2 q=0.5 dynamic max-weight rejection rmat N=2^24 deg=16, one walker per "
+                          "vertex, L=80"),
+    "metapath": dict(kind="rmat", n=1 << 24, deg=32, length=20, walkers=1 << 22, labels=5, schema=[0, 1, 2, 3, 4],
+                     name="metapath schema 0..4 dynamic ITS rmat N=2^24 deg=32, 5 labels, 2^22 random sources, L=20"),
 }
 
 
@@ -137,13 +142,15 @@ def build_inputs(wl, args, device):
     import torch
     from thunderrw_gb300 import generators as G
     n = 1 << args.scale if args.scale else wl["n"]
-    g = G.make_graph(wl["kind"], n, wl["deg"], seed=20240601, device=device, weights=wl["kind"] != "rmat",
-                     labels=0)
-    out = {"n": n, "row": g["row"], "adj": g["adj"], "weight": g["weight"]}
+    g = G.make_graph(wl["kind"], n, wl["deg"], seed=20240601, device=device,
+                     weights=wl["kind"] != "rmat" or "length" in wl, labels=wl.get("labels", 0))
+    out = {"n": n, "row": g["row"], "adj": g["adj"], "weight": g["weight"], "label": g["label"]}
     if "queries" in wl:
         q = args.queries or wl["queries"]
         out["sources"] = G.random_sources(g["row"], q, seed=7)
         out["per_query"] = wl["per_query"]
+    elif "walkers" in wl:
+        out["sources"] = G.random_sources(g["row"], wl["walkers"], seed=7)
     else:
         out["sources"] = G.all_sources(g["row"], seed=0)
     if torch.device(device).type == "cuda":
@@ -151,11 +158,11 @@ def build_inputs(wl, args, device):
     return out
 
 
-def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, threads):
+def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, threads, label=None):
     """The step-interleaved CPU port (oracle) on a bounded sample of the same
     workload, on all host threads.  Returns (steps/s, sample description)."""
     from oracle import oracle as O
-    og = O.Graph(row, adj, weight)
+    og = O.Graph(row, adj, weight, label)
     ncores = threads or os.cpu_count()
     if wl_name == "ppr":
         d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=wl["tp"], seed=11)
@@ -175,8 +182,14 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
             done_q += qs.size
         sample = "%d queries x %d walkers (%d steps) in %.1f s" % (done_q, per_query, total_steps, total_t)
         return total_steps / total_t, sample, ncores
-    og.build_tables("alias", 0)
-    d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=11)
+    if wl_name == "deepwalk":
+        og.build_tables("alias", 0)
+        d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=11)
+        interleaved = True
+    else:  # dynamic samplers: the plain per-walker port on all threads
+        d = O.make_desc(wl_name, "dynamic", "maxweight_rejection" if wl_name == "node2vec" else "its",
+                        length=wl["length"], p=wl.get("p", 1.0), q=wl.get("q", 1.0), schema=wl.get("schema"), seed=11)
+        interleaved = False
     src = np.asarray(sources, dtype=np.int32)
     total_steps, total_t, done = 0, 0.0, 0
     chunk = 1 << 16
@@ -184,7 +197,7 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
     while total_t < seconds and done < src.size:
         s = src[done:done + chunk]
         t0 = time.perf_counter()
-        r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=True, ring=64)
+        r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=interleaved, ring=64)
         total_t += time.perf_counter() - t0
         total_steps += r["steps"]
         done += s.size
@@ -255,7 +268,7 @@ def run_ours(args):
 
     wl = WORKLOADS[args.workload]
     inp = build_inputs(wl, args, dev)
-    graph = E.Graph(inp["row"], inp["adj"], inp["weight"])
+    graph = E.Graph(inp["row"], inp["adj"], inp["weight"], inp.get("label"))
     stream = torch.cuda.current_stream(dev)
     L = N.load()
     import ctypes
@@ -300,10 +313,14 @@ def run_ours(args):
         lengths = torch.empty(W, dtype=torch.int32, device=dev)
         steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
         counts = None
-        graph.build_tables("alias", "edge")
+        app = {"deepwalk": E.DeepWalk(Lw),
+               "node2vec": E.Node2Vec(Lw, wl.get("p", 2.0), wl.get("q", 0.5)),
+               "metapath": E.MetaPath(Lw, wl.get("schema", [0, 1, 2, 3, 4]))}[args.workload]
+        if args.workload == "deepwalk":
+            graph.build_tables("alias", "edge")
 
         def one_step(seed, engine="persistent"):
-            d = E.DeepWalk(Lw).desc(seed)
+            d = app.desc(seed)
             N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), W, 0,
                                ctypes.c_void_p(paths.data_ptr()), Lw, ctypes.c_void_p(lengths.data_ptr()), None,
                                ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
@@ -396,7 +413,7 @@ def run_ours(args):
                                     ctypes.c_void_p(stream.cuda_stream)))
             d2h += 8
         else:
-            d = E.DeepWalk(wl["length"]).desc(3000 + i)
+            d = app.desc(3000 + i)
             N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
                                ctypes.c_void_p(paths.data_ptr()), wl["length"], ctypes.c_void_p(lengths.data_ptr()),
                                None, ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
@@ -446,7 +463,18 @@ def run_ours(args):
 
     # ---- roofline of the walk kernel
     kmean = statistics.mean(kern_ms) / 1e3
-    bps = BYTES_PER_STEP[args.workload]
+    if args.workload in BYTES_PER_STEP:
+        bps = BYTES_PER_STEP[args.workload]
+    else:
+        # Algorithmic bytes per move from the oracle's sector-counting pass
+        # over the first 4096 walkers of this workload (same seeds).
+        from oracle import oracle as O
+        og = O.Graph(inp["row"], inp["adj"], inp["weight"], inp.get("label"))
+        d = O.make_desc(args.workload, app.mode, app.sampler, length=wl["length"], p=wl.get("p", 1.0),
+                        q=wl.get("q", 1.0), schema=wl.get("schema"), seed=2000)
+        nb, ns = O.count_bytes(og, d, src[:4096].cpu().numpy(), record_paths=True)
+        bps = nb / max(1, ns)
+        del og
     achieved = steps_per_batch * bps / kmean / 1e9
     peaks = {}
     try:
@@ -474,8 +502,9 @@ def run_ours(args):
         row = inp["row"].cpu().numpy()
         adj = inp["adj"].cpu().numpy()
         wt = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
+        lab = inp["label"].cpu().numpy() if inp.get("label") is not None else None
         v, sample, cores = cpu_baseline(args.workload, wl, row, adj, wt, src.cpu().numpy(),
-                                        inp.get("per_query", 0), args.cpu_seconds, 0)
+                                        inp.get("per_query", 0), args.cpu_seconds, 0, label=lab)
         cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": "step-interleaved C++ port of the reference ring, " + sample}
 

@@ -49,7 +49,7 @@ enum trw_status {
     TRW_ERR_BUSY = -8          /* serving queue full */
 };
 
-/* App hooks (random_walk/apps/*.cpp).  DeepWalk and GenericWalk share hooks:
+/* App hooks (random_walk/apps/<app>.cpp).  DeepWalk and GenericWalk share hooks:
  * weight = edge weight, update = (length == l), max_weight = 5.0. */
 enum trw_app {
     TRW_APP_DEEPWALK = 0,   /* deepwalk.cpp:9-30 */

@@ -18,6 +18,7 @@
 // libtrw_gpu.so.  Errors throw trw::Error (the reference asserts or exits).
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <fstream>

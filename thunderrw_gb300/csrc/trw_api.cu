@@ -332,9 +332,11 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
         // Automatic ring depth (launch-shape sweeps on GB300): one walker per
         // lane when visits go to sparse tables (their insert records cost
         // registers) or when there are too few walkers to give every lane
-        // several; four otherwise.
+        // several; two for max-weight rejection (its trial loop and
+        // neighbour search hold more state per walker: Node2Vec on R-MAT
+        // 2^24 runs 8.9e9 steps/s at two, 7.4e9 at four); four otherwise.
         const int64_t lanes = (int64_t)g->num_sms * 2048;
-        shape.ring = (table || num_walkers < 4 * lanes) ? 1 : 4;
+        shape.ring = (table || num_walkers < 4 * lanes) ? 1 : pl.sampler == kMaxRejection ? 2 : 4;
     }
     cudaError_t le;
     if (g->profile) {
@@ -413,7 +415,10 @@ int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *w
     chk(cudaMalloc(&d_row, sizeof(int64_t) * ((size_t)n + 1)));
     chk(cudaMalloc(&d_flags, 3 * sizeof(int)));
     if (weight) chk(cudaMalloc(&g->weight, sizeof(double) * es));
-    if (label) chk(cudaMalloc(&g->label, sizeof(int32_t) * es));
+    // labels padded to a multiple of 4 elements: the label ITS reads aligned 16-byte words
+    const size_t es4 = (es + 3) & ~(size_t)3;
+    if (label) chk(cudaMalloc(&g->label, sizeof(int32_t) * es4));
+    if (label) chk(cudaMemset(g->label, 0, sizeof(int32_t) * es4));
     chk(cudaMalloc(&g->state, sizeof(unsigned long long) * (2 * kEngineSlots + 1)));
     if (ce != cudaSuccess) { cudaFree(d_row); cudaFree(d_flags); return bail(fail(TRW_ERR_CUDA, "graph allocation: %s", cudaGetErrorString(ce))); }
     g->error = reinterpret_cast<int *>(g->state + 2 * kEngineSlots);

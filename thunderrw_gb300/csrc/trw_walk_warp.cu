@@ -111,28 +111,120 @@ __device__ int32_t its_select_double(const WalkParams &p, int32_t len, int32_t p
     return deg;  // unreachable for a positive total
 }
 
-// ITS over 0/1 label weights: rank floor(real2 * count) among the matches.
-__device__ int32_t its_select_label(const WalkParams &p, int32_t len, int2 crow, uint32_t u0) {
+// Label rows are read as 16-byte words from the aligned element a0 =
+// crow.x & ~3 (the label array is padded to a multiple of 4 elements), in
+// tiles of 128 elements (one int4 per lane) and kLabelUnroll tiles in flight
+// per lane.  Tiles are counted in at most kLabelGroups groups of whole load
+// rounds whose match counts stay in shared memory, so the selection pass
+// re-reads one group instead of the row.
+constexpr int kLabelUnroll = 8;
+constexpr int kLabelGroups = 256;
+
+// Matches of the 4 labels in v (elements e..e+3 counted from a0) that lie in
+// the row; bit k = element e + k.
+__device__ __forceinline__ uint32_t label_bits(int4 v, int32_t e, int32_t lo, int32_t span, int32_t want) {
+    uint32_t b = 0;
+    b |= (v.x == want && e + 0 >= lo && e + 0 < span) ? 1u : 0u;
+    b |= (v.y == want && e + 1 >= lo && e + 1 < span) ? 2u : 0u;
+    b |= (v.z == want && e + 2 >= lo && e + 2 < span) ? 4u : 0u;
+    b |= (v.w == want && e + 3 >= lo && e + 3 < span) ? 8u : 0u;
+    return b;
+}
+
+// ITS over 0/1 label weights: the reference's upper bound over the 0/1
+// prefix sums picks match number floor(count * real2) in row order.
+// gc: this warp's kLabelGroups counters in shared memory.
+__device__ int32_t its_select_label(const WalkParams &p, int32_t len, int2 crow, uint32_t u0, uint32_t *gc) {
     const int lane = threadIdx.x & 31;
-    const int32_t deg = crow.y - crow.x;
     const int32_t want = p.schema[(len - 1) % p.schema_len];
-    const int32_t *lab = p.g.label + crow.x;
-    uint32_t cnt = 0;
-    for (int32_t base = 0; base < deg; base += 32) {
-        const int32_t i = base + lane;
-        cnt += __popc(__ballot_sync(kFull, i < deg && __ldg(lab + i) == want));
+    const int32_t a0 = crow.x & ~3;
+    const int32_t lo = crow.x - a0;   // first row element, counted from a0
+    const int32_t span = crow.y - a0; // one past the last
+    const int32_t ntiles = (span + 127) >> 7;
+    constexpr int32_t kRound = kLabelUnroll * kLabelGroups;
+    const int32_t gs = kLabelUnroll * ((ntiles + kRound - 1) / kRound);  // tiles per group
+    const int4 *base = reinterpret_cast<const int4 *>(p.g.label + a0);
+    uint32_t total = 0;
+    for (int32_t t0 = 0; t0 < ntiles; t0 += kLabelUnroll) {
+        int4 v[kLabelUnroll];
+#pragma unroll
+        for (int u = 0; u < kLabelUnroll; ++u) {
+            const int32_t e = ((t0 + u) << 7) + (lane << 2);
+            v[u] = e < span ? __ldg(base + ((t0 + u) << 5) + lane) : make_int4(0, 0, 0, 0);
+        }
+        uint32_t c = 0;
+#pragma unroll
+        for (int u = 0; u < kLabelUnroll; ++u)
+            c += __popc(label_bits(v[u], ((t0 + u) << 7) + (lane << 2), lo, span, want));
+        const uint32_t tot = __reduce_add_sync(kFull, c);
+        if (lane == 0) {
+            const int32_t g = t0 / gs;
+            gc[g] = (t0 % gs == 0 ? 0u : gc[g]) + tot;
+        }
+        total += tot;
     }
-    if (cnt == 0) return -1;
-    const uint32_t m = (uint32_t)((double)cnt * real2(u0));  // floor of P[last] * dr_
+    if (total == 0) return -1;
+    const uint32_t m = (uint32_t)((double)total * real2(u0));  // floor of P[last] * dr_
+    __syncwarp();
+    // group holding match m: lane l sums groups 8l .. 8l+7, scan over lanes
+    const int32_t ng = (ntiles + gs - 1) / gs;
+    uint32_t own[kLabelGroups / 32];
+    uint32_t lsum = 0;
+#pragma unroll
+    for (int k = 0; k < kLabelGroups / 32; ++k) {
+        const int32_t g = lane * (kLabelGroups / 32) + k;
+        own[k] = g < ng ? gc[g] : 0u;
+        lsum += own[k];
+    }
+    __syncwarp();  // gc is rewritten by the next walker's count pass
+    uint32_t incl = lsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const unsigned hit = __ballot_sync(kFull, incl > m);
+    const int src = __ffs(hit) - 1;
+    int32_t grp = 0;
     uint32_t before = 0;
-    for (int32_t base = 0; base < deg; base += 32) {
-        const int32_t i = base + lane;
-        const unsigned b = __ballot_sync(kFull, i < deg && __ldg(lab + i) == want);
-        const uint32_t c = __popc(b);
-        if (before + c > m) return base + (int32_t)__fns(b, 0, (int)(m - before) + 1);
-        before += c;
+    if (lane == src) {
+        before = incl - lsum;
+        int kk = -1;
+#pragma unroll
+        for (int k = 0; k < kLabelGroups / 32; ++k) {  // constant indices keep own[] in registers
+            if (kk < 0) {
+                if (before + own[k] > m) kk = k;
+                else before += own[k];
+            }
+        }
+        grp = lane * (kLabelGroups / 32) + kk;
     }
-    return -1;  // unreachable
+    grp = __shfl_sync(kFull, grp, src);
+    before = __shfl_sync(kFull, before, src);
+    const int32_t tend = min((grp + 1) * gs, ntiles);
+    for (int32_t t = grp * gs; t < tend; ++t) {
+        const int32_t e = (t << 7) + (lane << 2);
+        const int4 v = e < span ? __ldg(base + (t << 5) + lane) : make_int4(0, 0, 0, 0);
+        const uint32_t b = label_bits(v, e, lo, span, want);
+        const uint32_t c = __popc(b);
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += y;
+        }
+        const uint32_t tile = __shfl_sync(kFull, x, 31);
+        if (before + tile > m) {
+            const uint32_t r = m - before;  // rank inside this tile
+            const bool mine = r >= x - c && r < x;
+            const unsigned who = __ballot_sync(kFull, mine);
+            int32_t sel = 0;
+            if (mine) sel = a0 + e + (int32_t)__fns(b, 0, (int)(r - (x - c)) + 1) - crow.x;
+            return __shfl_sync(kFull, sel, __ffs(who) - 1);
+        }
+        before += tile;
+    }
+    return -1;  // unreachable: group grp holds match m
 }
 
 // Row maximum of the hook weights (exact in any order).
@@ -246,6 +338,8 @@ template <int S, int U, int WK>
 __global__ void __launch_bounds__(kThreadBlock) walk_warp(const WalkParams p, int persistent) {
     const int lane = threadIdx.x & 31;
     const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    __shared__ uint32_t label_groups[WK == kLabelSchema ? kThreadBlock / 32 : 1][kLabelGroups];
+    uint32_t *gc = label_groups[WK == kLabelSchema ? threadIdx.x >> 5 : 0];
     AliasSlot *raw = nullptr, *tab = nullptr;
     if (S == kAlias) {
         raw = p.alias_scratch + warp_id * p.alias_scratch_stride;
@@ -298,7 +392,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_warp(const WalkParams p, in
             const int32_t deg = crow.y - crow.x;
             if (deg <= 0) continue;  // stops (my_nxt stays -1)
             if (S == kITS) {
-                const int32_t sel = WK == kLabelSchema ? its_select_label(p, len, crow, u0)
+                const int32_t sel = WK == kLabelSchema ? its_select_label(p, len, crow, u0, gc)
                                                        : its_select_double<WK>(p, len, prev, prow, crow, u0);
                 if (lane == j && sel >= 0) my_nxt = __ldg(p.g.adj + crow.x + sel);
             } else if (S == kRejection) {
