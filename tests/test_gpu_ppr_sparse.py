@@ -95,3 +95,72 @@ def test_sparse_capacity_and_reuse(rmat):
         np.testing.assert_array_equal(c, good.counts[:need].cpu().numpy())
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_sparse_host_ranges_match_device(rmat, pinned):
+    """With host outputs a large batch runs as several query ranges whose
+    copies overlap the next range's walk; the result equals the one-range
+    device-output batch entry for entry, and the oracle for sampled queries."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+    Q, wpq = 61, 160_000  # ~9.8 M walkers: 4 ranges of 16, 16, 16, 13 queries on 152 SMs
+    qs = G.random_sources(torch.from_numpy(rmat["row"]), Q, seed=8)
+    g = E.Graph(rmat["row"], rmat["adj"])
+    try:
+        dev = E.ppr_batch_sparse(g, qs, wpq, tp=0.2, seed=31)
+        need = int(dev.offsets[-1].item())
+        L = N.load()
+
+        def host(n, dtype):
+            t = torch.zeros(n, dtype=dtype)
+            return t.pin_memory() if pinned else t
+        off, v, c, steps = host(Q + 1, torch.int64), host(need, torch.int32), host(need, torch.int32), host(1, torch.int64)
+        src = qs.to(torch.int32).contiguous()
+        src = src.pin_memory() if pinned else src
+        d = E.PPR(0.2).desc(31)
+        rc = L.trw_ppr_batch_sparse(g.handle, ctypes.byref(d), src.data_ptr(), Q, wpq, off.data_ptr(), v.data_ptr(),
+                                    c.data_ptr(), need, steps.data_ptr(), 0, None)
+        assert rc == 0, L.trw_last_error()
+        assert int(steps[0]) == dev.steps
+        assert torch.equal(off, dev.offsets.cpu())
+        assert torch.equal(v, dev.vertices[:need].cpu())
+        assert torch.equal(c, dev.counts[:need].cpu())
+        og = O.Graph(rmat["row"], rmat["adj"])
+        for q in (0, 17, 60):  # first range, a middle range, the last (shorter) range
+            ref = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=31),
+                         qs.numpy()[q:q + 1], per_query=wpq, id_base=q * wpq, want_counts=True, want_lengths=False)
+            lo, hi = int(off[q]), int(off[q + 1])
+            dense = np.zeros(g.n, dtype=np.int32)
+            dense[v[lo:hi].numpy()] = c[lo:hi].numpy()
+            np.testing.assert_array_equal(dense, ref["counts"][0])
+    finally:
+        g.close()
+
+
+def test_sparse_order_with_wrapping_runs():
+    """Dense visits (every query reaches most of a 512-vertex graph) fill the
+    smallest tables to about half, so runs that wrap around the table end
+    are common; the output order must still be the same under both
+    schedules, and the counts the oracle's."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("er", 512, 48, seed=5, weights=False)
+    row, adj = g["row"].numpy(), g["adj"].numpy()
+    qs = G.random_sources(g["row"], 96, seed=6).numpy()
+    og = O.Graph(row, adj)
+    ref = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=9), qs, per_query=4000,
+                 want_counts=True, want_lengths=False)
+    gr = E.Graph(row, adj)
+    try:
+        a = E.ppr_batch_sparse(gr, qs, 4000, tp=0.2, seed=9, engine="persistent")
+        b = E.ppr_batch_sparse(gr, qs, 4000, tp=0.2, seed=9, engine="plain")
+        _check_against_dense(a, ref["counts"])
+        total = int(a.offsets[-1].item())
+        assert total > 96 * 256  # about half of each 1024-slot table is occupied
+        assert torch.equal(a.offsets, b.offsets)
+        assert torch.equal(a.vertices[:total], b.vertices[:total])
+        assert torch.equal(a.counts[:total], b.counts[:total])
+    finally:
+        gr.close()

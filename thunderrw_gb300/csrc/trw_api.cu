@@ -68,6 +68,7 @@ struct EngineSlot {
 };
 
 constexpr int kEngineSlots = 64;
+constexpr int kMaxRanges = 8;  // query ranges of a sparse PPR batch with host outputs
 
 int app_weight_kind(int app) {
     switch (app) {
@@ -119,6 +120,11 @@ struct trw_graph {
     bool have_post = false;
     DevBuf ppr_distinct;
     DevBuf stage_out;
+    // sparse PPR into host buffers: a copy stream, one event per query range
+    // and pinned words receiving each range's last offset
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t range_done[kMaxRanges] = {};
+    int64_t *h_ends = nullptr;
     std::mutex mu;
 };
 
@@ -132,6 +138,10 @@ void destroy_graph(trw_graph *g) {
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : g->range_done)
+        if (e) cudaEventDestroy(e);
+    if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
+    if (g->h_ends) cudaFreeHost(g->h_ends);
     delete g;
 }
 
@@ -539,14 +549,21 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         g->ppr_bits = bits;
         g->ppr_queries = num_queries;
     }
-    TRW_CUDA(g->ppr_distinct.ensure(sizeof(int32_t) * 17 * (size_t)std::max<int64_t>(1, num_queries)));
+    const size_t b_dist = align_up(sizeof(int32_t) * 17 * (size_t)std::max<int64_t>(1, num_queries));
+    TRW_CUDA(g->ppr_distinct.ensure(b_dist + sizeof(uint64_t) * (kMaxRanges + 1)));
     int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
     int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
+    uint64_t *d_steps = reinterpret_cast<uint64_t *>(static_cast<char *>(g->ppr_distinct.p) + b_dist);
 
-    // output staging for host buffers
+    // staging for host buffers: sources in; offsets, vertices, counts out
+    const bool h_src = num_queries > 0 && !is_device_ptr(sources);
     const bool h_off = !is_device_ptr(offsets);
     const bool h_v = vertices && !is_device_ptr(vertices);
     const bool h_c = counts && !is_device_ptr(counts);
+    const bool h_steps = steps && !is_device_ptr(steps);
+    const bool host_out = h_off || h_v || h_c;
+    const size_t b_src = h_src ? align_up(sizeof(int32_t) * (size_t)num_queries) : 0;
+    if (h_src) TRW_CUDA(g->stage.ensure(b_src));
     const size_t b_off = h_off ? align_up(sizeof(int64_t) * (size_t)(num_queries + 1)) : 0;
     const size_t b_v = h_v ? align_up(sizeof(int32_t) * (size_t)capacity) : 0;
     const size_t b_c = h_c ? align_up(sizeof(int32_t) * (size_t)capacity) : 0;
@@ -555,29 +572,86 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     int64_t *d_off = h_off ? reinterpret_cast<int64_t *>(ob) : offsets;
     int32_t *d_v = h_v ? reinterpret_cast<int32_t *>(ob + b_off) : vertices;
     int32_t *d_c = h_c ? reinterpret_cast<int32_t *>(ob + b_off + b_v) : counts;
+    const int32_t *d_src = sources;
+    if (h_src) {
+        d_src = static_cast<const int32_t *>(g->stage.p);
+        TRW_CUDA(cudaMemcpyAsync((void *)d_src, sources, sizeof(int32_t) * (size_t)num_queries,
+                                 cudaMemcpyHostToDevice, st));
+    }
 
+    // With host outputs the batch runs as up to kMaxRanges ranges of queries:
+    // while one range walks, the copy stream moves the previous range's
+    // entries to the host (a device-to-host copy runs at about half the rate
+    // the entries are produced, so it hides behind the next walk).  Every
+    // range keeps at least 8 walkers per lane of the GPU.
+    int ranges = 1;
+    if (host_out && num_queries > 1) {
+        const int64_t lanes = (int64_t)g->num_sms * 2048;
+        const int64_t by_walkers = num_queries * walkers_per_query / (8 * lanes);
+        ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kMaxRanges, num_queries), by_walkers));
+    }
+    if (host_out && !g->copy_stream) {
+        TRW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    }
+    if (host_out && !g->h_ends) TRW_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&g->h_ends),
+                                                       sizeof(int64_t) * kMaxRanges, cudaHostAllocDefault));
+    if (host_out)
+        for (cudaEvent_t &e : g->range_done)
+            if (!e) TRW_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+
+    // Walker ids continue across ranges (id_base = first query x walkers per
+    // query), so the walks do not depend on how the batch is split.
+    TRW_CUDA(cudaMemsetAsync(d_off, 0, sizeof(int64_t), st));
+    const int64_t per = num_queries > 0 ? (num_queries + ranges - 1) / ranges : 0;
+    int nr = 0;
     g->ppr_dirty = true;
-    int rc = run_walk(g, desc, sources, num_queries, num_queries * walkers_per_query, walkers_per_query, 0, nullptr,
-                      0, nullptr, nullptr, 0, false, steps, engine, st, tables, bits, /*hold_lock=*/true);
-    if (rc) return rc;
-    TRW_CUDA(launch_ppr_offsets(tables, bits, distinct, num_queries, d_off, st));
-    TRW_CUDA(launch_ppr_emit(tables, bits, num_queries, d_off, distinct, d_v, d_c, capacity, g->error, st));
+    for (int64_t qs = 0; qs < num_queries; qs += per, ++nr) {
+        const int64_t nq = std::min(per, num_queries - qs);
+        int32_t *tab = tables + (qs << (bits + 1));
+        int32_t *dist = distinct + 17 * qs;
+        int rc = run_walk(g, desc, d_src + qs, nq, nq * walkers_per_query, walkers_per_query, qs * walkers_per_query,
+                          nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, st, tab, bits,
+                          /*hold_lock=*/true);
+        if (rc) return rc;
+        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, st));
+        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, st));
+        if (host_out) {
+            TRW_CUDA(cudaMemcpyAsync(g->h_ends + nr, d_off + qs + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            TRW_CUDA(cudaEventRecord(g->range_done[nr], st));
+        }
+    }
     TRW_CUDA(cudaEventRecord(g->ppr_done, st));
     g->ppr_dirty = false;
     if (g->profile) {
         TRW_CUDA(cudaEventRecord(g->ev_post1, st));
         g->have_post = true;
     }
-    if (h_off || h_v || h_c) {
-        TRW_CUDA(cudaStreamSynchronize(st));
-        int64_t total = 0;
-        TRW_CUDA(cudaMemcpy(&total, d_off + num_queries, sizeof(int64_t), cudaMemcpyDeviceToHost));
-        if (h_off) TRW_CUDA(cudaMemcpy(offsets, d_off, sizeof(int64_t) * (size_t)(num_queries + 1), cudaMemcpyDeviceToHost));
-        const size_t ent = (size_t)std::min(total, capacity);
-        if (total <= capacity && ent) {
-            if (h_v) TRW_CUDA(cudaMemcpy(vertices, d_v, sizeof(int32_t) * ent, cudaMemcpyDeviceToHost));
-            if (h_c) TRW_CUDA(cudaMemcpy(counts, d_c, sizeof(int32_t) * ent, cudaMemcpyDeviceToHost));
+    if (steps) {
+        uint64_t *sum = h_steps ? d_steps + kMaxRanges : steps;
+        if (nr == 1) TRW_CUDA(cudaMemcpyAsync(sum, d_steps, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        else TRW_CUDA(launch_sum_steps(d_steps, nr, sum, st));
+        if (h_steps) TRW_CUDA(cudaMemcpyAsync(steps, sum, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    }
+    int64_t total = 0;
+    if (host_out) {
+        int64_t prev = 0;
+        for (int r = 0; r < nr; ++r) {
+            TRW_CUDA(cudaEventSynchronize(g->range_done[r]));
+            const int64_t end = g->h_ends[r];
+            total = end;
+            if (end <= capacity && end > prev) {
+                const size_t n = sizeof(int32_t) * (size_t)(end - prev);
+                if (h_v) TRW_CUDA(cudaMemcpyAsync(vertices + prev, d_v + prev, n, cudaMemcpyDeviceToHost, g->copy_stream));
+                if (h_c) TRW_CUDA(cudaMemcpyAsync(counts + prev, d_c + prev, n, cudaMemcpyDeviceToHost, g->copy_stream));
+            }
+            prev = end;
         }
+    }
+    if (host_out || h_src || h_steps) {
+        TRW_CUDA(cudaStreamSynchronize(st));
+        if (h_off) TRW_CUDA(cudaMemcpyAsync(offsets, d_off, sizeof(int64_t) * (size_t)(num_queries + 1),
+                                            cudaMemcpyDeviceToHost, g->copy_stream));
+        if (host_out) TRW_CUDA(cudaStreamSynchronize(g->copy_stream));
         int err = 0;
         TRW_CUDA(cudaMemcpy(&err, g->error, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) {
@@ -585,7 +659,8 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
             if (err & kErrCapacity)
                 return fail(TRW_ERR_CAPACITY, "sparse PPR output needs %lld entries, capacity is %lld",
                             (long long)total, (long long)capacity);
-            return fail(TRW_ERR_DEVICE, "device error word %d", err);
+            return fail(TRW_ERR_DEVICE, "device error word %d (1 = rejection trial limit, 2 = invalid source vertex)",
+                        err);
         }
     }
     return TRW_OK;

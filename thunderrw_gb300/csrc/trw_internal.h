@@ -28,12 +28,15 @@ cudaError_t launch_walk_warp(const WalkParams &p, int sampler, int update, int w
 // number of per-warp dynamic-alias scratch tables the warp engine will use
 int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
 
+// offsets[0] must hold the entries before this range of queries (0 for the first)
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st);
 // `distinct` holds nq totals followed by nq x 16 segment counts
 cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
                             const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
                             cudaStream_t st);
+// *out = parts[0] + ... + parts[n-1], on the device
+cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st);
 
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);

@@ -10,13 +10,15 @@
 // After the walk:
 //  * distinct_kernel + offsets_kernel: occupied slots per query, then their
 //    exclusive scan into CSR offsets (offsets[q] .. offsets[q+1] hold query
-//    q's entries);
+//    q's entries), continuing from offsets[0] so that a batch can run as
+//    several ranges of queries;
 //  * emit_kernel (one CTA per query): writes the (vertex, count) pairs.  With
 //    linear probing the SET of occupied slots does not depend on the order of
 //    insertion, only the order of keys inside each run of occupied slots
-//    does; so the kernel emits slots in order with the keys inside each run
-//    sorted, which makes the output a function of the visit counts alone.
-//    It then zeroes the table for the next batch.
+//    does; so the kernel emits runs in slot order (the run that wraps around
+//    the table end last) with the keys inside each run sorted, which makes
+//    the output a function of the visit counts alone.  It then zeroes the
+//    table for the next batch.
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
@@ -82,9 +84,11 @@ __global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *t
     }
 }
 
+// offsets[0] holds the entries of the queries before this range (0 for the
+// first range of a batch); offsets[1..nq] become the running totals.
 __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *distinct, int64_t nq, int64_t *offsets) {
     __shared__ int64_t sums[32];
-    int64_t carry = 0;
+    int64_t carry = offsets[0];  // read by every thread before the first write below
     for (int64_t b = 0; b < nq; b += kScanThreads) {
         const int64_t i = b + threadIdx.x;
         const int64_t v = i < nq ? (int64_t)distinct[i] : 0;
@@ -96,76 +100,125 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
     if (threadIdx.x == 0) offsets[nq] = carry;
 }
 
-constexpr uint32_t kRing = 8;   // staged 32-slot blocks per warp
-constexpr uint32_t kAhead = 3;  // blocks staged ahead of the one being emitted
-
-// One CTA per query, one contiguous segment of the table per warp.  Output
-// order: slots in index order, the keys of each run of occupied slots sorted
-// (runs end at the end of the table).  Which slots are occupied does not
-// depend on the insertion order, so this order depends on the counts alone.
-// Every occupied slot finds its own output position:
-//   pos = (occupied slots before it) - (its distance back to the run start)
-//         + (rank of its key among the run's keys)
-// A warp walks its segment 32 slots at a time with coalesced loads, keeping a
-// ring of staged blocks in shared memory so that run neighbours within one
-// block behind and kAhead blocks ahead are read from there; farther ones
-// (rare) come from global memory, which stays intact until the final zeroing.
+// One CTA per query, one contiguous segment of the table per warp.
+//
+// Output order.  Inserts probe linearly and wrap from the last slot to slot
+// 0, so the occupied slots form maximal runs on a cycle; which slots are
+// occupied, and which keys each run holds, do not depend on the order of the
+// inserts, only the order of the keys inside a run does.  The entries are
+// written run by run in slot order, each run's keys sorted, except that the
+// run wrapping around the table end (if any) comes last.  Each occupied slot
+// finds its own output position:
+//   pos = (occupied slots before it) - (slots of the wrapping run at the table
+//         start) - (its distance back to the run start) + (rank of its key
+//         among the run's keys)
+// A warp walks its segment 32 slots at a time with coalesced loads and keeps
+// the previous, current and next blocks of keys in registers (two more blocks
+// in flight): the run of a slot is found from the three occupancy ballots and
+// its key ranked against the run through shuffles.  Runs reaching beyond that
+// 96-slot window, and the wrapping run, are read from global memory, which
+// stays intact until the final zeroing.
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, const int64_t *offsets,
                                                             const int32_t *seg_counts, int32_t *vout, int32_t *cout,
                                                             int64_t capacity, int *error) {
-    __shared__ int32_t ring[kEmitWarps][kRing * 32];
-    __shared__ int32_t cring[kEmitWarps][kRing * 32];
+    __shared__ uint32_t wrap[2];
     const int64_t q = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nslots = 1u << bits;
     int32_t *keys = tables + (q << (bits + 1));
     int32_t *cnts = keys + nslots;
-    const bool write = offsets[q + 1] <= capacity;
-    if (!write && threadIdx.x == 0) atomicOr(error, kErrCapacity);
+    const int64_t end = offsets[q + 1];
+    const bool write = end <= capacity;
+    if (threadIdx.x == 0) {
+        if (!write) atomicOr(error, kErrCapacity);
+        // the wrapping run: `head` slots from slot 0 and `tail` slots before the end
+        uint32_t head = 0, tail = 0;
+        if (__ldg(keys) != 0 && __ldg(keys + nslots - 1) != 0) {
+            while (head < nslots && __ldg(keys + head) != 0) ++head;
+            if (head < nslots) {
+                while (__ldg(keys + nslots - 1 - tail) != 0) ++tail;
+            } else {
+                head = 0;  // a full table (the walk reported it) has no run boundary
+            }
+        }
+        wrap[0] = head;
+        wrap[1] = tail;
+    }
+    __syncthreads();
+    const uint32_t head = wrap[0], tail = wrap[1], cyc = head + tail;
     int64_t prefix = offsets[q];
     for (int w = 0; w < warp; ++w) prefix += seg_counts[q * kEmitWarps + w];
 
     const uint32_t seg = nslots / kEmitWarps;  // >= 64: tables have >= 1024 slots
     const uint32_t lo = warp * seg, nblk = seg / 32;
-    int32_t *rk = ring[warp];
-    int32_t *rc = cring[warp];
-    // block j of the segment lives in ring slot j % kRing, block -1 in the last slot
-    auto stage = [&](uint32_t j) {
-        const uint32_t x = lo + j * 32 + lane;
-        const int k = x < nslots ? __ldg(keys + x) : 0;
-        rk[(j % kRing) * 32 + lane] = k;
-        rc[(j % kRing) * 32 + lane] = k ? __ldg(cnts + x) : 0;
-    };
-    rk[(kRing - 1) * 32 + lane] = lo ? __ldg(keys + lo - 32 + lane) : 0;
-    for (uint32_t j = 0; j < kAhead; ++j) stage(j);
+    const uint32_t x0 = lo + lane;
+    auto key_at = [&](uint32_t y) { return y < nslots ? __ldg(keys + y) : 0; };
+    auto cnt_at = [&](uint32_t y) { return y < nslots ? __ldg(cnts + y) : 0; };
+    int32_t kp = lo ? __ldg(keys + lo - 32 + lane) : 0;
+    int32_t kc = key_at(x0), cc = cnt_at(x0);
+    int32_t kn = key_at(x0 + 32), cn = cnt_at(x0 + 32);
+    int32_t k2 = key_at(x0 + 64), c2 = cnt_at(x0 + 64);
+    unsigned op = __ballot_sync(0xffffffffu, kp != 0);
+    const unsigned lt = lanemask_lt(), le = lt | (1u << lane);
     for (uint32_t b = 0; b < nblk; ++b) {
-        const uint32_t x0 = lo + b * 32, x = x0 + lane;
-        stage(b + kAhead);
-        __syncwarp();
-        const int key = rk[(b % kRing) * 32 + lane];
-        const unsigned occm = __ballot_sync(0xffffffffu, key != 0);
-        const int64_t before = prefix + __popc(occm & ((1u << lane) - 1u));
-        prefix += __popc(occm);
-        if (write && key != 0) {
-            const uint32_t slo = x0 >= 32 ? x0 - 32 : 0, shi = x0 + (kAhead + 1) * 32;
-            auto nkey = [&](uint32_t y) {
-                if (y >= slo && y < shi) return rk[((y - lo) / 32 % kRing) * 32 + (y & 31)];
-                return y < nslots ? __ldg(keys + y) : 0;
-            };
-            uint32_t back = 0;
-            while (x > back && nkey(x - back - 1) != 0) ++back;
-            uint32_t rank = 0;
-            for (uint32_t d = 1; d <= back; ++d) rank += nkey(x - d) < key;
-            for (uint32_t y = x + 1; y < nslots; ++y) {
-                const int k2 = nkey(y);
-                if (k2 == 0) break;
-                rank += k2 < key;
-            }
-            const int64_t pos = before - back + rank;
-            vout[pos] = key - 1;
-            cout[pos] = rc[(b % kRing) * 32 + lane];
+        const uint32_t x = x0 + b * 32;
+        const int32_t k3 = key_at(x + 96), c3 = cnt_at(x + 96);
+        const unsigned oc = __ballot_sync(0xffffffffu, kc != 0), on = __ballot_sync(0xffffffffu, kn != 0);
+        const int64_t before = prefix + __popc(oc & lt);
+        prefix += __popc(oc);
+        const bool in_wrap = kc != 0 && (x < head || x >= nslots - tail);
+        // window positions: 0-31 previous block, 32-63 this block, 64-95 next block
+        int s = -1, e = -1;
+        if (kc != 0 && !in_wrap) {
+            const unsigned zb = ~oc & lt, za = ~oc & ~le;
+            if (zb) s = 64 - __clz(zb);
+            else if (~op) s = 32 - __clz(~op);
+            if (za) e = 31 + __ffs(za);
+            else if (~on) e = 63 + __ffs(~on);
         }
-        __syncwarp();
+        const bool fast = s >= 0 && e >= 0;
+        const int len = fast ? e - s : 0;
+        const int maxlen = __reduce_max_sync(0xffffffffu, len);
+        uint32_t rank = 0;
+        for (int d = 0; d < maxlen; ++d) {
+            const int j = s + d;
+            const int src = j & 31;
+            const int32_t a = __shfl_sync(0xffffffffu, kp, src);
+            const int32_t m = __shfl_sync(0xffffffffu, kc, src);
+            const int32_t n = __shfl_sync(0xffffffffu, kn, src);
+            const int32_t k = j < 32 ? a : j < 64 ? m : n;
+            if (d < len && j != 32 + lane) rank += k < kc;
+        }
+        if (write && kc != 0) {
+            int64_t pos;
+            if (fast) {
+                pos = before - head - (32 + lane - s) + rank;
+            } else if (in_wrap) {
+                rank = 0;
+                for (uint32_t i = 0; i < cyc; ++i) {
+                    const uint32_t y = i < tail ? nslots - tail + i : i - tail;
+                    rank += __ldg(keys + y) < kc;
+                }
+                pos = end - cyc + rank;
+            } else {
+                uint32_t back = 0;
+                while (x > back && __ldg(keys + x - back - 1) != 0) ++back;
+                rank = 0;
+                for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + x - d) < kc;
+                for (uint32_t y = x + 1; y < nslots; ++y) {
+                    const int32_t k = __ldg(keys + y);
+                    if (k == 0) break;
+                    rank += k < kc;
+                }
+                pos = before - head - back + rank;
+            }
+            vout[pos] = kc - 1;
+            cout[pos] = cc;
+        }
+        kp = kc; op = oc;
+        kc = kn; cc = cn;
+        kn = k2; cn = c2;
+        k2 = k3; c2 = c3;
     }
     if (threadIdx.x == 0) {
         int64_t t = 0;
@@ -178,7 +231,19 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     for (uint32_t i = threadIdx.x; i < nslots / 2; i += blockDim.x) z[i] = make_int4(0, 0, 0, 0);
 }
 
+__global__ void sum_steps_kernel(const unsigned long long *parts, int n, unsigned long long *out) {
+    unsigned long long t = 0;
+    for (int i = 0; i < n; ++i) t += parts[i];
+    *out = t;
+}
+
 }  // namespace
+
+cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st) {
+    sum_steps_kernel<<<1, 1, 0, st>>>(reinterpret_cast<const unsigned long long *>(parts), n,
+                                      reinterpret_cast<unsigned long long *>(out));
+    return cudaGetLastError();
+}
 
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st) {
