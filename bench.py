@@ -138,6 +138,16 @@ class ClockSampler:
 # workload construction
 # ---------------------------------------------------------------------------
 
+def workload_name(wl, args):
+    """The workload's name, with any size override spelled out."""
+    over = []
+    if args.scale:
+        over.append("N=2^%d" % args.scale)
+    if args.queries:
+        over.append("%d queries" % args.queries)
+    return wl["name"] + (" [reduced: %s]" % ", ".join(over) if over else "")
+
+
 def build_inputs(wl, args, device):
     import torch
     from thunderrw_gb300 import generators as G
@@ -240,7 +250,7 @@ def run_reference(args):
         "impl": "reference", "metric": "walk_steps_per_s", "value": value, "unit": "steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
-        "config": {"workload": wl["name"]},
+        "config": {"workload": workload_name(wl, args)},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
                          "sample": "step-interleaved C++ port of the reference ring (64 walkers per thread), "
                                    "per step " + sample},
@@ -395,30 +405,38 @@ def run_ours(args):
         h_off = torch.empty(Q + 1, dtype=torch.int64).pin_memory()
         h_vert = torch.empty(cap, dtype=torch.int32).pin_memory()
         h_vcnt = torch.empty(cap, dtype=torch.int32).pin_memory()
+    elif args.workload != "ppr":
+        h_paths = torch.empty((W, wl["length"]), dtype=torch.int32).pin_memory()  # the walks' result
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_steps, d2h = 0, 0
-    for i in range(args.steps):
+
+    def e2e_step(i):
         if args.workload == "ppr" and sparse:
             d = E.PPR(wl["tp"]).desc(3000 + i)
             N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
                                            ctypes.c_void_p(h_off.data_ptr()), ctypes.c_void_p(h_vert.data_ptr()),
                                            ctypes.c_void_p(h_vcnt.data_ptr()), cap, ctypes.c_void_p(h_steps.data_ptr()),
                                            0, ctypes.c_void_p(stream.cuda_stream)))
-            d2h += 8 * (Q + 1) + 8 * int(h_off[-1].item()) + 8
+            return int(h_steps.item()), 8 * (Q + 1) + 8 * int(h_off[-1].item()) + 8
         elif args.workload == "ppr":
             d = E.PPR(wl["tp"]).desc(3000 + i)
             N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
                                     ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(h_steps.data_ptr()), 1, 0,
                                     ctypes.c_void_p(stream.cuda_stream)))
-            d2h += 8
-        else:
-            d = app.desc(3000 + i)
-            N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
-                               ctypes.c_void_p(paths.data_ptr()), wl["length"], ctypes.c_void_p(lengths.data_ptr()),
-                               None, ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
-            d2h += 8
-        e2e_steps += int(h_steps.item())
+            return int(h_steps.item()), 8
+        d = app.desc(3000 + i)
+        N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
+                           ctypes.c_void_p(h_paths.data_ptr()), wl["length"], None, None,
+                           ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
+        return int(h_steps.item()), h_paths.numel() * 4 + 8
+
+    e2e_step(-1)  # untimed: the first host-buffer call allocates its staging and copy streams
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps, d2h = 0, 0
+    for i in range(args.steps):
+        s_i, b_i = e2e_step(i)
+        e2e_steps += s_i
+        d2h += b_i
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
     e2e = {"value": e2e_steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": int(h_src.numel() * 4),
@@ -489,7 +507,8 @@ def run_ours(args):
     import glob
     import re
     for md in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        m = re.search(r"traffic_bytes_per_step_%s = ([0-9.]+)" % args.workload, open(md).read())
+        key = "ppr_dense" if args.workload == "ppr" and not sparse else args.workload
+        m = re.search(r"traffic_bytes_per_step_%s = ([0-9.]+)" % key, open(md).read())
         if m:
             traffic = float(m.group(1)) * steps_per_batch
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -514,7 +533,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
             "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": wl["name"], "n": graph.n, "e": graph.e,
+            "config": {"workload": workload_name(wl, args), "n": graph.n, "e": graph.e,
                        "steps_per_batch": steps_per_batch, "engine": "persistent",
                        "counts": ("dense int32 [Q][N], zeroed every step" if args.workload == "ppr" and not sparse
                                   else "sparse CSR per query (offsets, vertex, int32 count)")

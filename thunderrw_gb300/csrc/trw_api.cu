@@ -68,7 +68,7 @@ struct EngineSlot {
 };
 
 constexpr int kEngineSlots = 64;
-constexpr int kMaxRanges = 8;  // query ranges of a sparse PPR batch with host outputs
+constexpr int kMaxRanges = 16;  // query ranges of a sparse PPR batch with host outputs
 
 int app_weight_kind(int app) {
     switch (app) {
@@ -120,10 +120,12 @@ struct trw_graph {
     bool have_post = false;
     DevBuf ppr_distinct;
     DevBuf stage_out;
-    // sparse PPR into host buffers: a copy stream, one event per query range
-    // and pinned words receiving each range's last offset
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t range_done[kMaxRanges] = {};
+    // sparse PPR into host buffers: a second compute stream and a copy
+    // stream, per-range events (offsets scanned, range finished) and pinned
+    // words receiving each range's last offset
+    cudaStream_t aux_stream = nullptr, copy_stream = nullptr;
+    cudaEvent_t range_done[kMaxRanges] = {}, offsets_done[kMaxRanges] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t *h_ends = nullptr;
     std::mutex mu;
 };
@@ -138,8 +140,13 @@ void destroy_graph(trw_graph *g) {
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
         if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : g->range_done)
-        if (e) cudaEventDestroy(e);
+    for (int r = 0; r < kMaxRanges; ++r) {
+        if (g->range_done[r]) cudaEventDestroy(g->range_done[r]);
+        if (g->offsets_done[r]) cudaEventDestroy(g->offsets_done[r]);
+    }
+    if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+    if (g->ev_join) cudaEventDestroy(g->ev_join);
+    if (g->aux_stream) cudaStreamDestroy(g->aux_stream);
     if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
     if (g->h_ends) cudaFreeHost(g->h_ends);
     delete g;
@@ -242,6 +249,20 @@ int make_plan(const trw_graph *g, const trw_walk_desc *d, Plan &pl) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Largest v in [0, 2^32) with real1(v) = RN(v * RN(1 / (2^32 - 1))) <= t, for
+// t >= 0.  real1 is monotonic in v, so the device compares the draw with
+// this integer instead of converting it (same product, same rounding).
+uint32_t real1_threshold(double t) {
+    const double c = 1.0 / 4294967295.0;
+    uint64_t lo = 0, hi = 0xffffffffull;  // real1(lo) <= t holds for t >= 0
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo + 1) / 2;
+        volatile double r = (double)mid * c;
+        if (r <= t) lo = mid; else hi = mid - 1;
+    }
+    return (uint32_t)lo;
+}
+
 // Shared implementation of trw_walk and trw_ppr_batch.
 int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
              int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
@@ -317,6 +338,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
     p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
     p.tp = desc->tp;
+    p.tp_max = real1_threshold(desc->tp);
     p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
                  : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
     p.seed = desc->seed;
@@ -582,43 +604,62 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     // With host outputs the batch runs as up to kMaxRanges ranges of queries:
     // while one range walks, the copy stream moves the previous range's
     // entries to the host (a device-to-host copy runs at about half the rate
-    // the entries are produced, so it hides behind the next walk).  Every
-    // range keeps at least 8 walkers per lane of the GPU.
+    // the entries are produced, so it hides behind the next walk).  Ranges
+    // alternate between two compute streams so that the next range's walk
+    // fills the GPU while the last walkers of a range finish; only the
+    // offsets scans are chained across ranges.  Every range keeps at least 8
+    // walkers per lane of the GPU.
     int ranges = 1;
     if (host_out && num_queries > 1) {
         const int64_t lanes = (int64_t)g->num_sms * 2048;
         const int64_t by_walkers = num_queries * walkers_per_query / (8 * lanes);
         ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kMaxRanges, num_queries), by_walkers));
     }
-    if (host_out && !g->copy_stream) {
-        TRW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (host_out) {
+        if (!g->copy_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+        if (!g->aux_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
+        if (!g->h_ends) TRW_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&g->h_ends), sizeof(int64_t) * kMaxRanges,
+                                               cudaHostAllocDefault));
+        for (cudaEvent_t *e : {&g->ev_fork, &g->ev_join})
+            if (!*e) TRW_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        for (int r = 0; r < kMaxRanges; ++r) {
+            if (!g->range_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->range_done[r], cudaEventDisableTiming));
+            if (!g->offsets_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->offsets_done[r], cudaEventDisableTiming));
+        }
     }
-    if (host_out && !g->h_ends) TRW_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&g->h_ends),
-                                                       sizeof(int64_t) * kMaxRanges, cudaHostAllocDefault));
-    if (host_out)
-        for (cudaEvent_t &e : g->range_done)
-            if (!e) TRW_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 
     // Walker ids continue across ranges (id_base = first query x walkers per
     // query), so the walks do not depend on how the batch is split.
     TRW_CUDA(cudaMemsetAsync(d_off, 0, sizeof(int64_t), st));
     const int64_t per = num_queries > 0 ? (num_queries + ranges - 1) / ranges : 0;
+    const cudaStream_t rs[2] = {st, ranges > 1 ? g->aux_stream : st};
+    if (rs[1] != st) {
+        TRW_CUDA(cudaEventRecord(g->ev_fork, st));
+        TRW_CUDA(cudaStreamWaitEvent(rs[1], g->ev_fork, 0));
+    }
     int nr = 0;
     g->ppr_dirty = true;
     for (int64_t qs = 0; qs < num_queries; qs += per, ++nr) {
         const int64_t nq = std::min(per, num_queries - qs);
+        const cudaStream_t sr = rs[nr & 1];
         int32_t *tab = tables + (qs << (bits + 1));
         int32_t *dist = distinct + 17 * qs;
         int rc = run_walk(g, desc, d_src + qs, nq, nq * walkers_per_query, walkers_per_query, qs * walkers_per_query,
-                          nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, st, tab, bits,
+                          nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, sr, tab, bits,
                           /*hold_lock=*/true);
         if (rc) return rc;
-        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, st));
-        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, st));
+        if (nr > 0 && rs[1] != st) TRW_CUDA(cudaStreamWaitEvent(sr, g->offsets_done[nr - 1], 0));
+        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, sr));
+        if (host_out) TRW_CUDA(cudaEventRecord(g->offsets_done[nr], sr));
+        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, sr));
         if (host_out) {
-            TRW_CUDA(cudaMemcpyAsync(g->h_ends + nr, d_off + qs + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-            TRW_CUDA(cudaEventRecord(g->range_done[nr], st));
+            TRW_CUDA(cudaMemcpyAsync(g->h_ends + nr, d_off + qs + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, sr));
+            TRW_CUDA(cudaEventRecord(g->range_done[nr], sr));
         }
+    }
+    if (rs[1] != st) {
+        TRW_CUDA(cudaEventRecord(g->ev_join, rs[1]));
+        TRW_CUDA(cudaStreamWaitEvent(st, g->ev_join, 0));
     }
     TRW_CUDA(cudaEventRecord(g->ppr_done, st));
     g->ppr_dirty = false;
@@ -811,6 +852,7 @@ extern "C" int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc 
     p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
     p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
     p.tp = desc->tp;
+    p.tp_max = real1_threshold(desc->tp);
     p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
                  : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
     p.seed = desc->seed;

@@ -96,6 +96,7 @@ struct WalkParams {
     int32_t length;       // l_
     int32_t schema_len;
     double p_w, q_w, n2v_max, tp, max_weight;
+    uint32_t tp_max;  // largest draw v with real1(v) <= tp (real1 is monotonic in v)
     uint64_t seed;
     int32_t static_unit;  // static rejection with unit weights (PPR)
     int32_t schema[kMaxSchema];
@@ -197,7 +198,7 @@ template <int U>
 __device__ __forceinline__ bool app_update(const WalkParams &p, uint64_t wid, int32_t len) {
     if (U == kFixedLength) return len == p.length;
     const uint4 t = draw_block(p.seed, wid, (uint32_t)len, kTermBlock);
-    return real1(t.x) <= p.tp;
+    return t.x <= p.tp_max;  // == (real1(t.x) <= p.tp), without the FP64 pipe
 }
 
 // Utility::upper_bound_branchless (utility.h:18-27): number of entries <= t.
