@@ -121,6 +121,11 @@ int trw_graph_destroy(trw_graph *g);
 /* num_vertices / num_edges / max_degree (graph.h:152-166). */
 int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degree);
 
+/* Waits until all work the library enqueued for this graph, on any stream,
+ * has finished (the reference's compute and static_initialization return
+ * only when done; asynchronous callers use this as the join point). */
+int trw_graph_synchronize(trw_graph *g);
+
 /* ---- static tables ---------------------------------------------------- */
 
 /* Replaces static_initialization (creeper.h:102-175) and the offline

@@ -192,6 +192,34 @@ inline void generate_single_source(const Graph &g, std::vector<WalkerMeta> &walk
     for (int i = 0; i < count; ++i) walkers.push_back({i, u, u, 1, nullptr});
 }
 
+// generate_random_source (walker_generator.cpp:27-40): `count` walkers from
+// uniformly drawn vertices with at least one neighbour.  The reference draws
+// with SFMT seeded by `seed`; this draws from the library's Philox stream
+// (draw j = word j%4 of block (j/4, 0, 0xffffffff, 0xffffffff) under key
+// (seed, 0)), so the sources differ from the reference's as every walk does.
+inline uint32_t philox_word(uint64_t seed, uint64_t j) {
+    uint32_t c[4] = {(uint32_t)(j >> 2), 0u, 0xffffffffu, 0xffffffffu};
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        c[0] = n0; c[1] = (uint32_t)p1; c[2] = n2; c[3] = (uint32_t)p0;
+    }
+    return c[j & 3];
+}
+
+inline void generate_random_source(const Graph &g, std::vector<WalkerMeta> &walkers, int count, uint64_t seed = 0) {
+    walkers.clear();
+    bool any = false;
+    for (int32_t v = 0; v < g.num_vertices() && !any; ++v) any = g.degree(v) != 0;
+    if (!any) return;
+    for (uint64_t j = 0; (int)walkers.size() < count; ++j) {
+        const int32_t u = (int32_t)(philox_word(seed, j) % (uint32_t)g.num_vertices());
+        if (g.degree(u) != 0) walkers.push_back({(int)walkers.size(), u, u, 1, nullptr});
+    }
+}
+
 struct Result {
     uint64_t steps = 0;
     std::vector<int32_t> paths;    // walkers x path_cap, -1 padded

@@ -6,6 +6,8 @@
   the reference tree with the Philox ``SFMT.h`` shim (ref_harness.cpp).  Built
   only where the reference tree exists; the binaries never leave this machine
   as source and are git-ignored.
+* ``oracle/_ref/edgelist_to_csr``: the reference's EdgeList2CSR tool, same
+  terms.
 """
 from __future__ import annotations
 
@@ -47,10 +49,21 @@ def ref_cmds(reference_root):
     return cmds
 
 
+def ref_tool_cmds(reference_root):
+    """The reference's EdgeList2CSR tool (toolset/edgelist_to_csr.cpp over
+    util/graph/graph.cpp), the checker of thunderrw_gb300/toolset.py."""
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    return [["g++", "-O2", "-std=c++14", "-include", "cstdint", "-w", "-I", reference_root,
+             os.path.join(reference_root, "toolset", "edgelist_to_csr.cpp"),
+             os.path.join(reference_root, "util", "graph", "graph.cpp"),
+             "-o", os.path.join(out_dir, "edgelist_to_csr"), "-pthread"]]
+
+
 def build(reference_root="/root/reference", with_ref=True):
     cmds = [oracle_cmd()]
     if with_ref and os.path.isdir(os.path.join(reference_root, "random_walk")):
-        cmds += ref_cmds(reference_root)
+        cmds += ref_cmds(reference_root) + ref_tool_cmds(reference_root)
     _run(cmds)
 
 

@@ -54,5 +54,30 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     return LIB
 
 
+CLI_SRC = os.path.join(HERE, "cli", "trw_app.cpp")
+BIN_DIR = os.path.join(HERE, "bin")
+CLI_APPS = ["deepwalk", "ppr", "node2vec", "metapath", "genericwalk"]  # trw_app values 0..4
+
+
+def build_cli() -> list:
+    """The reference's app programs over libtrw_gpu.so: bin/<app>, one g++
+    process per app, in parallel (host code only; no CUDA headers)."""
+    os.makedirs(BIN_DIR, exist_ok=True)
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    procs, outs = [], []
+    for i, app in enumerate(CLI_APPS):
+        out = os.path.join(BIN_DIR, app)
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++14", "-O2", "-Wall", "-DTRW_CLI_APP=%d" % i, "-I", inc,
+               CLI_SRC, "-o", out, "-L", HERE, "-ltrw_gpu", "-Wl,-rpath,$ORIGIN/.."]
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        outs.append(out)
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("g++ failed: %s\n%s" % (" ".join(cmd), out.decode(errors="replace")))
+    return outs
+
+
 if __name__ == "__main__":
     print(build(verbose=True, ptxas_verbose="-v" in sys.argv))
+    print("\n".join(build_cli()))

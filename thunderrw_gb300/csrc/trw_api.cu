@@ -500,6 +500,13 @@ int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degr
     return TRW_OK;
 }
 
+int trw_graph_synchronize(trw_graph *g) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    TRW_CUDA(cudaSetDevice(g->device));
+    TRW_CUDA(cudaDeviceSynchronize());
+    return TRW_OK;
+}
+
 int trw_tables_build(trw_graph *g, int32_t sampler, int32_t weight_kind, trw_stream_t stream) {
     if (!g) return fail(TRW_ERR_INVALID, "null graph");
     if (weight_kind != TRW_WEIGHTS_EDGE && weight_kind != TRW_WEIGHTS_UNIT) return fail(TRW_ERR_INVALID, "bad weight kind");
