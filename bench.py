@@ -30,6 +30,8 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+from thunderrw_gb300 import replicas  # noqa: E402
+
 BYTES_PER_STEP = {
     # Algorithmic bytes per move (32-byte sectors of each independent random
     # access, 4 bytes per path entry): row pair 32 + adjacency entry 32 +
@@ -72,10 +74,7 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return replicas.rank_env()
 
 
 # ---------------------------------------------------------------------------
@@ -148,7 +147,8 @@ def workload_name(wl, args):
     return wl["name"] + (" [reduced: %s]" % ", ".join(over) if over else "")
 
 
-def build_inputs(wl, args, device):
+def build_inputs(wl, args, device, rank=0):
+    """The workload's graph (the same on every rank) and rank's own sources."""
     import torch
     from thunderrw_gb300 import generators as G
     n = 1 << args.scale if args.scale else wl["n"]
@@ -157,10 +157,10 @@ def build_inputs(wl, args, device):
     out = {"n": n, "row": g["row"], "adj": g["adj"], "weight": g["weight"], "label": g["label"]}
     if "queries" in wl:
         q = args.queries or wl["queries"]
-        out["sources"] = G.random_sources(g["row"], q, seed=7)
+        out["sources"] = G.random_sources(g["row"], q, seed=replicas.replica_seed(7, rank) & 0x7FFFFFFF)
         out["per_query"] = wl["per_query"]
     elif "walkers" in wl:
-        out["sources"] = G.random_sources(g["row"], wl["walkers"], seed=7)
+        out["sources"] = G.random_sources(g["row"], wl["walkers"], seed=replicas.replica_seed(7, rank) & 0x7FFFFFFF)
     else:
         out["sources"] = G.all_sources(g["row"], seed=0)
     if torch.device(device).type == "cuda":
@@ -277,7 +277,7 @@ def run_ours(args):
     from thunderrw_gb300 import engine as E
 
     wl = WORKLOADS[args.workload]
-    inp = build_inputs(wl, args, dev)
+    inp = build_inputs(wl, args, dev, rank)
     graph = E.Graph(inp["row"], inp["adj"], inp["weight"], inp.get("label"))
     stream = torch.cuda.current_stream(dev)
     L = N.load()
@@ -301,7 +301,7 @@ def run_ours(args):
             counts = None
 
             def one_step(seed, engine="persistent"):
-                d = E.PPR(wl["tp"]).desc(seed)
+                d = E.PPR(wl["tp"]).desc(replicas.replica_seed(seed, rank))
                 N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q,
                                                per_q, ctypes.c_void_p(offsets.data_ptr()),
                                                ctypes.c_void_p(vert.data_ptr()), ctypes.c_void_p(vcnt.data_ptr()), cap,
@@ -311,7 +311,7 @@ def run_ours(args):
             counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
 
             def one_step(seed, engine="persistent"):
-                d = E.PPR(wl["tp"]).desc(seed)
+                d = E.PPR(wl["tp"]).desc(replicas.replica_seed(seed, rank))
                 N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q, per_q,
                                         ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(steps_dev.data_ptr()),
                                         1, N.ENGINES[engine], ctypes.c_void_p(stream.cuda_stream)))
@@ -330,7 +330,7 @@ def run_ours(args):
             graph.build_tables("alias", "edge")
 
         def one_step(seed, engine="persistent"):
-            d = app.desc(seed)
+            d = app.desc(replicas.replica_seed(seed, rank))
             N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), W, 0,
                                ctypes.c_void_p(paths.data_ptr()), Lw, ctypes.c_void_p(lengths.data_ptr()), None,
                                ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
@@ -387,15 +387,7 @@ def run_ours(args):
     graph.profile(False)
     clocks = sampler.stop()
     steps_per_batch = total_steps / args.steps
-    if world > 1:
-        t = torch.tensor([t_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
-        s = torch.tensor([steps_per_batch * args.steps], device=dev, dtype=torch.float64)
-        dist.all_reduce(s)
-        all_steps = float(s.item())
-    else:
-        all_steps = steps_per_batch * args.steps
+    t_total, all_steps = replicas.reduce_timing(t_total, steps_per_batch * args.steps, world, dev)
     value = all_steps / t_total
 
     # ---- e2e: through the C ABI with host buffers (pinned sources in, results out)
@@ -411,19 +403,19 @@ def run_ours(args):
 
     def e2e_step(i):
         if args.workload == "ppr" and sparse:
-            d = E.PPR(wl["tp"]).desc(3000 + i)
+            d = E.PPR(wl["tp"]).desc(replicas.replica_seed(3000 + i, rank))
             N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
                                            ctypes.c_void_p(h_off.data_ptr()), ctypes.c_void_p(h_vert.data_ptr()),
                                            ctypes.c_void_p(h_vcnt.data_ptr()), cap, ctypes.c_void_p(h_steps.data_ptr()),
                                            0, ctypes.c_void_p(stream.cuda_stream)))
             return int(h_steps.item()), 8 * (Q + 1) + 8 * int(h_off[-1].item()) + 8
         elif args.workload == "ppr":
-            d = E.PPR(wl["tp"]).desc(3000 + i)
+            d = E.PPR(wl["tp"]).desc(replicas.replica_seed(3000 + i, rank))
             N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
                                     ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(h_steps.data_ptr()), 1, 0,
                                     ctypes.c_void_p(stream.cuda_stream)))
             return int(h_steps.item()), 8
-        d = app.desc(3000 + i)
+        d = app.desc(replicas.replica_seed(3000 + i, rank))
         N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
                            ctypes.c_void_p(h_paths.data_ptr()), wl["length"], None, None,
                            ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
