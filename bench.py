@@ -181,8 +181,9 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
         counts.fill(1)  # touch every page once, outside the timed passes
         total_steps, total_t, done_q = 0, 0.0, 0
         src = np.asarray(sources, dtype=np.int32)
-        while total_t < seconds and done_q < src.size:
-            qs = src[done_q:done_q + chunk]
+        while total_t < seconds:  # the batch again (fresh walker ids) until the budget is spent
+            at = done_q % src.size
+            qs = src[at:at + chunk]
             t0 = time.perf_counter()
             counts[: qs.size].fill(0)
             r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_lengths=False,
@@ -190,7 +191,8 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
             total_t += time.perf_counter() - t0
             total_steps += r["steps"]
             done_q += qs.size
-        sample = "%d queries x %d walkers (%d steps) in %.1f s" % (done_q, per_query, total_steps, total_t)
+        sample = "%d queries x %d walkers (%d steps, %.2f passes over the batch) in %.1f s" % (
+            done_q, per_query, total_steps, done_q / src.size, total_t)
         return total_steps / total_t, sample, ncores
     if wl_name == "deepwalk":
         og.build_tables("alias", 0)
@@ -204,8 +206,11 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
     total_steps, total_t, done = 0, 0.0, 0
     chunk = 1 << 16
     paths = None
-    while total_t < seconds and done < src.size:
-        s = src[done:done + chunk]
+    # chunks of the workload's walkers in order; a workload that finishes
+    # before the time budget runs again (fresh walker ids) until it is spent
+    while total_t < seconds:
+        at = done % src.size
+        s = src[at:at + chunk]
         t0 = time.perf_counter()
         r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=interleaved, ring=64)
         total_t += time.perf_counter() - t0
@@ -213,8 +218,8 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
         done += s.size
         paths = r["paths"]
     del paths
-    return total_steps / total_t, "%d walkers x %d steps (%d steps) in %.1f s" % (
-        done, wl["length"] - 1, total_steps, total_t), ncores
+    return total_steps / total_t, "%d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
+        done, wl["length"] - 1, total_steps, done / src.size, total_t), ncores
 
 
 # ---------------------------------------------------------------------------

@@ -363,12 +363,13 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     if (shape.ring == 0) {
         // Automatic ring depth (launch-shape sweeps on GB300): one walker per
         // lane when visits go to sparse tables (their insert records cost
-        // registers) or when there are too few walkers to give every lane
-        // several; two for max-weight rejection (its trial loop and
-        // neighbour search hold more state per walker: Node2Vec on R-MAT
-        // 2^24 runs 8.9e9 steps/s at two, 7.4e9 at four); four otherwise.
+        // registers), for max-weight rejection (its trial loop and neighbour
+        // search hold more state per walker: Node2Vec on R-MAT 2^24 with
+        // paths takes 65.2 ms at one, 72.0 ms at two, 78 ms at four) and
+        // when there are too few walkers to give every lane several; four
+        // otherwise.
         const int64_t lanes = (int64_t)g->num_sms * 2048;
-        shape.ring = (table || num_walkers < 4 * lanes) ? 1 : pl.sampler == kMaxRejection ? 2 : 4;
+        shape.ring = (table || pl.sampler == kMaxRejection || num_walkers < 4 * lanes) ? 1 : 4;
     }
     cudaError_t le;
     if (g->profile) {
