@@ -249,6 +249,20 @@ int make_plan(const trw_graph *g, const trw_walk_desc *d, Plan &pl) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Largest u in [0, 2^32) with real2(u) * m = RN(u * 2^-32 * m) <= w (the
+// max-weight rejection test), for m, w >= 0: the product is monotonic in u,
+// so the device accepts a draw by comparing it with this integer.
+uint32_t accept_threshold(double m, double w) {
+    uint64_t lo = 0, hi = 0xffffffffull;  // u = 0 gives 0 <= w
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo + 1) / 2;
+        volatile double r = (double)mid * (1.0 / 4294967296.0);
+        volatile double y = r * m;
+        if (y <= w) lo = mid; else hi = mid - 1;
+    }
+    return (uint32_t)lo;
+}
+
 // Largest v in [0, 2^32) with real1(v) = RN(v * RN(1 / (2^32 - 1))) <= t, for
 // t >= 0.  real1 is monotonic in v, so the device compares the draw with
 // this integer instead of converting it (same product, same rounding).
@@ -261,6 +275,26 @@ uint32_t real1_threshold(double t) {
         if (r <= t) lo = mid; else hi = mid - 1;
     }
     return (uint32_t)lo;
+}
+
+// The app's hook parameters and the integer forms of its acceptance tests.
+void fill_app_params(WalkParams &p, const trw_walk_desc *desc) {
+    p.length = desc->length;
+    p.schema_len = desc->app == TRW_APP_METAPATH ? desc->schema_len : 1;
+    if (desc->app == TRW_APP_METAPATH)
+        for (int i = 0; i < desc->schema_len; ++i) p.schema[i] = desc->schema[i];
+    // node2vec.cpp:176-178,227,234: weights 1/p (return), 1 (common neighbour), 1/q
+    p.p_w = desc->p != 0.0 ? 1.0 / desc->p : 0.0;
+    p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
+    p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
+    // max_weight hooks: node2vec.cpp:198-205, ppr.cpp/metapath.cpp 1, deepwalk/genericwalk 5
+    p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
+                 : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
+    p.tp = desc->tp;
+    p.tp_max = real1_threshold(desc->tp);
+    const double w[4] = {p.n2v_max, p.p_w, 1.0, p.q_w};  // n2v_class order; [2] is PPR's unit weight
+    for (int k = 0; k < 4; ++k) p.accept_max[k] = accept_threshold(p.max_weight, w[k]);
+    p.seed = desc->seed;
 }
 
 // Shared implementation of trw_walk and trw_ppr_batch.
@@ -329,19 +363,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     WalkParams p;
     std::memset(&p, 0, sizeof p);
     p.g = dev_view(g);
-    p.length = desc->length;
-    p.schema_len = desc->app == TRW_APP_METAPATH ? desc->schema_len : 1;
-    if (desc->app == TRW_APP_METAPATH)
-        for (int i = 0; i < desc->schema_len; ++i) p.schema[i] = desc->schema[i];
-    // node2vec.cpp:176-178,227,234: weights 1/p (return), 1 (common neighbour), 1/q
-    p.p_w = desc->p != 0.0 ? 1.0 / desc->p : 0.0;
-    p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
-    p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
-    p.tp = desc->tp;
-    p.tp_max = real1_threshold(desc->tp);
-    p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
-                 : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
-    p.seed = desc->seed;
+    fill_app_params(p, desc);
     p.static_unit = pl.table_kind == TRW_WEIGHTS_UNIT;
     p.sources = d_src;
     p.num_walkers = num_walkers;
@@ -852,18 +874,7 @@ extern "C" int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc 
     WalkParams p;
     std::memset(&p, 0, sizeof p);
     p.g = dev_view(g);
-    p.length = desc->length;
-    p.schema_len = desc->app == TRW_APP_METAPATH ? desc->schema_len : 1;
-    if (desc->app == TRW_APP_METAPATH)
-        for (int i = 0; i < desc->schema_len; ++i) p.schema[i] = desc->schema[i];
-    p.p_w = desc->p != 0.0 ? 1.0 / desc->p : 0.0;
-    p.q_w = desc->q != 0.0 ? 1.0 / desc->q : 0.0;
-    p.n2v_max = std::max(1.0, std::max(p.q_w, p.p_w));
-    p.tp = desc->tp;
-    p.tp_max = real1_threshold(desc->tp);
-    p.max_weight = desc->app == TRW_APP_NODE2VEC ? p.n2v_max
-                 : (desc->app == TRW_APP_PPR || desc->app == TRW_APP_METAPATH) ? 1.0 : 5.0;
-    p.seed = desc->seed;
+    fill_app_params(p, desc);
     p.sources = sources;
     p.num_walkers = num_walkers;
     p.id_base = id_base;

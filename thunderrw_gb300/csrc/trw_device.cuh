@@ -55,6 +55,21 @@ struct DrawCursor {
 __device__ __forceinline__ double real1(uint32_t v) { return (double)v * (1.0 / 4294967295.0); }
 __device__ __forceinline__ double real2(uint32_t v) { return (double)v * (1.0 / 4294967296.0); }
 
+// real2(u) <= x without the FP64 pipe (GB300 issues one warp-wide FP64
+// instruction per 64 cycles per SM sub-partition).  real2(u) = u * 2^-32
+// exactly, so the test is u <= floor(x * 2^32), read off x's IEEE fields.
+__device__ __forceinline__ bool real2_le(uint32_t u, double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+    if (b >> 63) return u == 0 && (b << 1) == 0;  // x < 0: never; x = -0.0: u = 0 only
+    if (e == 0x7FFu) return frac == 0;            // +inf: always; NaN: never
+    if (e >= 1023u) return true;                  // x >= 1 > real2(u)
+    const unsigned long long m = e ? (frac | (1ull << 52)) : frac;
+    const uint32_t shift = 1043u - (e ? e : 1u);  // x * 2^32 = m * 2^-shift
+    return (unsigned long long)u <= (shift >= 64u ? 0ull : m >> shift);
+}
+
 // ---------------------------------------------------------------------------
 // Graph view in HBM.
 //   rows[v]  = (row_ptr[v], row_ptr[v+1]) as one 8-byte pair: a single aligned
@@ -97,6 +112,10 @@ struct WalkParams {
     int32_t schema_len;
     double p_w, q_w, n2v_max, tp, max_weight;
     uint32_t tp_max;  // largest draw v with real1(v) <= tp (real1 is monotonic in v)
+    // max-weight rejection with walker-independent weight values (Node2Vec's
+    // n2v_max, 1/p, 1, 1/q; PPR's 1): accept <=> draw u <= accept_max[k] with
+    // k the weight's class, the largest u with real2(u) * max_weight <= w_k
+    uint32_t accept_max[4];
     uint64_t seed;
     int32_t static_unit;  // static rejection with unit weights (PPR)
     int32_t schema[kMaxSchema];
@@ -191,6 +210,17 @@ __device__ __forceinline__ double app_weight(const WalkParams &p, int32_t len, i
     if (nbr == prev) return p.p_w;
     const int2 rn = __ldg(p.g.rows + nbr);
     return is_neighbor(p.g, prev, prev_row, nbr, rn) ? 1.0 : p.q_w;
+}
+
+// Node2Vec's weight as a class index into accept_max: 0 n2v_max (first move),
+// 1 return (1/p), 2 common neighbour (1), 3 otherwise (1/q); the same cases
+// as app_weight<kNode2Vec>.
+__device__ __forceinline__ int n2v_class(const WalkParams &p, int32_t len, int32_t prev, int2 prev_row,
+                                         int32_t nbr) {
+    if (len == 1) return 0;
+    if (nbr == prev) return 1;
+    const int2 rn = __ldg(p.g.rows + nbr);
+    return is_neighbor(p.g, prev, prev_row, nbr, rn) ? 2 : 3;
 }
 
 // The update hook: length_ == l_, or PPR's real1(termination draw) <= tp.

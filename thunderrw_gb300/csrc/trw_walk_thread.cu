@@ -185,7 +185,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
             const int32_t deg = s[r].crow.y - s[r].crow.x;
             if (deg > 0) {
                 const AliasSlot a = load_alias(g.alias + s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg));
-                nxt[r] = real2(rnd[r].y) <= a.prob ? a.first : a.second;
+                nxt[r] = real2_le(rnd[r].y, a.prob) ? a.first : a.second;
                 moved[r] = true;
             }
         }
@@ -268,9 +268,17 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
             for (;;) {
                 const int32_t p0 = (int32_t)(c.next() % (uint32_t)deg);
                 nb = __ldg(g.adj + s[r].crow.x + p0);
-                const double w = app_weight<WK>(p, s[r].len, s[r].prev, s[r].prow, nb, s[r].crow.x + p0);
-                const double y = real2(c.next()) * p.max_weight;
-                if (y <= w) break;
+                bool accept;
+                if (WK == kNode2Vec) {
+                    const int k = n2v_class(p, s[r].len, s[r].prev, s[r].prow, nb);
+                    accept = c.next() <= p.accept_max[k];
+                } else if (WK == kUnitWeight) {
+                    accept = c.next() <= p.accept_max[2];
+                } else {
+                    const double w = app_weight<WK>(p, s[r].len, s[r].prev, s[r].prow, nb, s[r].crow.x + p0);
+                    accept = real2(c.next()) * p.max_weight <= w;
+                }
+                if (accept) break;
                 if (++trials >= kMaxTrials) break;
             }
             if (trials >= kMaxTrials) { atomicOr(p.error, kErrTrials); continue; }

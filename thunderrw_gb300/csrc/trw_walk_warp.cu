@@ -331,7 +331,7 @@ __device__ int32_t alias_draw(const WalkParams &p, int32_t len, int32_t prev, in
     __syncwarp();
     const uint32_t p0 = u0 % (uint32_t)deg;
     const AliasSlot s = tab[p0];
-    return real2(u1) <= s.prob ? s.first : s.second;
+    return real2_le(u1, s.prob) ? s.first : s.second;
 }
 
 template <int S, int U, int WK>
