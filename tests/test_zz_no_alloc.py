@@ -98,3 +98,36 @@ def test_noalloc_rejects_host_pointers_and_rows_above_its_limit():
         assert rc == -1  # TRW_ERR_INVALID: staging a host buffer would allocate
     finally:
         small.close()
+
+
+def test_noalloc_node2vec_before_edge_set():
+    """The first Node2Vec walk on a graph builds its edge set; the
+    allocation-free entry point never does, so called first it runs the
+    binary-search neighbour test.  Both forms must give the same walks."""
+    from tests.gpu_util import need_gpu
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+
+    g = G.make_graph("rmat", 1 << 12, 12, seed=78)
+    graph = E.Graph(g["row"], g["adj"])
+    try:
+        L = 20
+        app = E.Node2Vec(L, 2.0, 0.5, sampler="alias")
+        src = G.all_sources(g["row"], seed=4)[:2000].cuda()
+        W = src.numel()
+        f = _entry(N)
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        paths = torch.full((W, L), -7, dtype=torch.int32, device="cuda")
+        lengths = torch.full((W,), -7, dtype=torch.int32, device="cuda")
+        steps = torch.zeros(1, dtype=torch.int64, device="cuda")
+        d = app.desc(6)
+        rc = f(graph.handle, ctypes.byref(d), _ptr(src), W, 0, _ptr(paths), L, _ptr(lengths), None, _ptr(steps),
+               stream)
+        assert rc == 0, N.load().trw_last_error()
+        ref = E.compute(graph, src, app, seed=6)  # builds the edge set
+        torch.cuda.synchronize()
+        assert torch.equal(paths, ref.paths) and torch.equal(lengths, ref.lengths)
+        assert int(steps.item()) == ref.steps
+    finally:
+        graph.close()

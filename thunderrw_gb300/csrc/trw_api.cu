@@ -96,6 +96,12 @@ struct trw_graph {
     double *prefix = nullptr;
     double *rmax = nullptr;
     int alias_kind = -1, prefix_kind = -1, rmax_kind = -1;
+    // Node2Vec's edge set (built by its first walk); edge_state 0 = not yet,
+    // 1 = built, -1 = no room for it (the walks then binary-search the lists)
+    unsigned long long *edges = nullptr;
+    int32_t edge_bits = 0;
+    int32_t edge_symmetric = 0;
+    int edge_state = 0;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
     unsigned long long *state = nullptr;
     int *error = nullptr;
@@ -135,7 +141,7 @@ namespace {
 void destroy_graph(trw_graph *g) {
     if (!g) return;
     cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
-    cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state);
+    cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state); cudaFree(g->edges);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
@@ -156,7 +162,43 @@ DevGraph dev_view(const trw_graph *g) {
     DevGraph d;
     d.rows = g->rows; d.adj = g->adj; d.weight = g->weight; d.label = g->label;
     d.alias = g->alias; d.prefix = g->prefix; d.rmax = g->rmax; d.n = g->n; d.e = g->e;
+    d.edges = g->edge_state == 1 ? g->edges : nullptr;
+    d.edge_bits = g->edge_bits;
+    d.edge_symmetric = g->edge_symmetric;
     return d;
+}
+
+// Node2Vec's neighbour test as one hash probe instead of a binary search:
+// the set of directed edges, at most two-thirds full (2^bits >= 1.5 e).  If
+// the device has no room for it the walks keep the binary search.
+int build_edge_set(trw_graph *g, cudaStream_t st) {
+    if (g->edge_state != 0 || g->e <= 0) return TRW_OK;
+    int32_t bits = 10;
+    while (bits < 32 && (double)(1ull << bits) < 1.5 * (double)g->e) ++bits;
+    if (bits > 31) { g->edge_state = -1; return TRW_OK; }
+    const size_t bytes = sizeof(unsigned long long) << bits;
+    size_t free_b = 0, total_b = 0;
+    TRW_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes + (size_t(1) << 30) > free_b || cudaMalloc(&g->edges, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        g->edges = nullptr;
+        g->edge_state = -1;
+        return TRW_OK;
+    }
+    int *d_sym = nullptr;
+    TRW_CUDA(cudaMalloc(&d_sym, sizeof(int)));
+    const int one = 1;
+    TRW_CUDA(cudaMemcpyAsync(d_sym, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+    TRW_CUDA(cudaMemsetAsync(g->edges, 0xFF, bytes, st));
+    TRW_CUDA(launch_build_edge_set(dev_view(g), g->edges, bits, d_sym, st));
+    int sym = 0;
+    TRW_CUDA(cudaMemcpyAsync(&sym, d_sym, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    cudaFree(d_sym);
+    g->edge_bits = bits;
+    g->edge_symmetric = sym;
+    g->edge_state = 1;
+    return TRW_OK;
 }
 
 int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
@@ -320,6 +362,11 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
             if (rc) return rc;
         }
         TRW_CUDA(cudaStreamWaitEvent(st, g->tables_done, 0));  // built on another stream, perhaps
+    }
+
+    if (desc->app == TRW_APP_NODE2VEC && g->edge_state == 0) {
+        rc = build_edge_set(g, st);
+        if (rc) return rc;
     }
 
     // Stage host buffers.

@@ -281,6 +281,58 @@ __global__ void validate_kernel(const int64_t *row, const int32_t *adj, int32_t 
 
 inline unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+constexpr int kEdgeRun = 8;  // consecutive CSR entries per thread in the edge-set kernels
+
+// Source vertex of CSR entry i: the largest v with rows[v].x <= i (rows of
+// zero length share their start with the next row, so this is the row that
+// holds i).
+__device__ __forceinline__ int32_t row_of(const DevGraph &g, int64_t i) {
+    int32_t lo = 0, hi = g.n - 1;
+    while (lo < hi) {
+        const int32_t mid = lo + ((hi - lo + 1) >> 1);
+        if ((int64_t)__ldg(&g.rows[mid].x) <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Inserts every directed edge (v, adj[i]) into the set.  Each thread takes
+// kEdgeRun consecutive entries: one search for the first entry's row, then
+// it walks forward row by row.
+__global__ void build_edge_set_kernel(DevGraph g, unsigned long long *set, int32_t bits) {
+    const uint32_t mask = (1u << bits) - 1u;
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kEdgeRun;
+    if (first >= g.e) return;
+    int32_t v = row_of(g, first);
+    int2 r = __ldg(g.rows + v);
+    const int64_t last = min(first + kEdgeRun, g.e);
+    for (int64_t i = first; i < last; ++i) {
+        while (i >= r.y) r = __ldg(g.rows + ++v);
+        const unsigned long long k = edge_key(v, __ldg(g.adj + i));
+        uint32_t h = edge_slot(k, bits);
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            const unsigned long long old = atomicCAS(set + h, kEdgeEmpty, k);
+            if (old == kEdgeEmpty || old == k) break;
+            h = (h + 1) & mask;
+        }
+    }
+}
+
+// Clears *symmetric if some edge's reverse is missing.
+__global__ void edge_symmetry_kernel(DevGraph g, int *symmetric) {
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kEdgeRun;
+    if (first >= g.e) return;
+    int32_t v = row_of(g, first);
+    int2 r = __ldg(g.rows + v);
+    const int64_t last = min(first + kEdgeRun, g.e);
+    for (int64_t i = first; i < last; ++i) {
+        while (i >= r.y) r = __ldg(g.rows + ++v);
+        if (!edge_exists(g, __ldg(g.adj + i), v)) {
+            atomicAnd(symmetric, 0);
+            return;
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st) {
@@ -300,6 +352,18 @@ cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaSt
 cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_max_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, int32_t bits, int *symmetric,
+                                  cudaStream_t st) {
+    if (g.e <= 0) return cudaSuccess;
+    const unsigned grid = blocks_for((g.e + kEdgeRun - 1) / kEdgeRun);
+    build_edge_set_kernel<<<grid, 256, 0, st>>>(g, set, bits);
+    DevGraph gs = g;
+    gs.edges = set;
+    gs.edge_bits = bits;
+    edge_symmetry_kernel<<<grid, 256, 0, st>>>(gs, symmetric);
     return cudaGetLastError();
 }
 

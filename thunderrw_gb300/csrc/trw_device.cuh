@@ -92,9 +92,41 @@ struct DevGraph {
     const AliasSlot *alias;
     const double *prefix;
     const double *rmax;
+    // Node2Vec's neighbour test: an open-addressing set of the directed edges
+    // (u, v) as (u << 32 | v), 2^edge_bits slots, kEdgeEmpty = free; null
+    // until the first Node2Vec walk builds it.  edge_symmetric: every edge's
+    // reverse is present.
+    const unsigned long long *edges;
+    int32_t edge_bits;
+    int32_t edge_symmetric;
     int32_t n;
     int64_t e;
 };
+
+constexpr unsigned long long kEdgeEmpty = ~0ull;  // (0xffffffff, 0xffffffff) is no edge: ids < 2^31
+
+__device__ __forceinline__ unsigned long long edge_key(int32_t u, int32_t v) {
+    return ((unsigned long long)(uint32_t)u << 32) | (uint32_t)v;
+}
+
+__device__ __forceinline__ uint32_t edge_slot(unsigned long long k, int32_t bits) {
+    return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> (64 - bits));
+}
+
+// Whether the directed edge (u, v) exists (u's list holds v).  The set is at
+// most two-thirds full, so a free slot ends every probe sequence.
+__device__ __forceinline__ bool edge_exists(const DevGraph &g, int32_t u, int32_t v) {
+    const unsigned long long k = edge_key(u, v);
+    const uint32_t mask = (1u << g.edge_bits) - 1u;
+    uint32_t h = edge_slot(k, g.edge_bits);
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long x = __ldg(g.edges + h);
+        if (x == k) return true;
+        if (x == kEdgeEmpty) return false;
+        h = (h + 1) & mask;
+    }
+    return false;
+}
 
 enum Sampler : int { kUniform = 0, kITS = 1, kAlias = 2, kRejection = 3, kMaxRejection = 4 };
 enum Update : int { kFixedLength = 0, kGeometric = 1 };
@@ -196,6 +228,23 @@ __device__ __forceinline__ bool is_neighbor(const DevGraph &g, int32_t u, int2 r
     return false;
 }
 
+// is_neighbor(prev, nbr) as Node2Vec's hook calls it (node2vec.cpp:186-193).
+// With the edge set: on a symmetric graph the answer is edge (prev, nbr); on
+// others the reference's choice of list (the lower-degree endpoint's,
+// graph.h:181-183) needs both degrees, then one lookup.  Without it: the
+// binary search.
+__device__ __forceinline__ bool n2v_neighbor(const DevGraph &g, int32_t prev, int2 prev_row, int32_t nbr) {
+    if (g.edges) {
+        if (g.edge_symmetric) return edge_exists(g, prev, nbr);
+        const int2 rn = __ldg(g.rows + nbr);
+        // is_neighbor(u = prev, v = nbr): swap if deg(u) < deg(v), then look for u in v's list
+        const bool swap = (prev_row.y - prev_row.x) < (rn.y - rn.x);
+        return swap ? edge_exists(g, prev, nbr) : edge_exists(g, nbr, prev);
+    }
+    const int2 rn = __ldg(g.rows + nbr);
+    return is_neighbor(g, prev, prev_row, nbr, rn);
+}
+
 // The weight hook of the app (node2vec.cpp:182-196, metapath.cpp:22-30,
 // deepwalk.cpp:19-21, ppr.cpp:95-97) for the edge (cur -> nbr) at eid.
 // `len` and `prev` are the walker's length_ and seq_[length_-2].
@@ -208,8 +257,7 @@ __device__ __forceinline__ double app_weight(const WalkParams &p, int32_t len, i
     // Node2Vec
     if (len == 1) return p.n2v_max;
     if (nbr == prev) return p.p_w;
-    const int2 rn = __ldg(p.g.rows + nbr);
-    return is_neighbor(p.g, prev, prev_row, nbr, rn) ? 1.0 : p.q_w;
+    return n2v_neighbor(p.g, prev, prev_row, nbr) ? 1.0 : p.q_w;
 }
 
 // Node2Vec's weight as a class index into accept_max: 0 n2v_max (first move),
@@ -219,8 +267,7 @@ __device__ __forceinline__ int n2v_class(const WalkParams &p, int32_t len, int32
                                          int32_t nbr) {
     if (len == 1) return 0;
     if (nbr == prev) return 1;
-    const int2 rn = __ldg(p.g.rows + nbr);
-    return is_neighbor(p.g, prev, prev_row, nbr, rn) ? 2 : 3;
+    return n2v_neighbor(p.g, prev, prev_row, nbr) ? 2 : 3;
 }
 
 // The update hook: length_ == l_, or PPR's real1(termination draw) <= tp.

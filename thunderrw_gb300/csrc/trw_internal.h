@@ -39,6 +39,10 @@ cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int
 cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st);
 
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
+// Node2Vec's edge set: `set` (2^bits slots) must hold kEdgeEmpty everywhere;
+// *symmetric must hold 1 and is cleared if some edge's reverse is missing.
+cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, int32_t bits, int *symmetric,
+                                  cudaStream_t st);
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);
 cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st);
 cudaError_t launch_validate_graph(const int64_t *row, const int32_t *adj, int32_t n, int64_t e, int check_sorted,

@@ -180,14 +180,23 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
         const int len = fast ? e - s : 0;
         const int maxlen = __reduce_max_sync(0xffffffffu, len);
         uint32_t rank = 0;
-        for (int d = 0; d < maxlen; ++d) {
-            const int j = s + d;
-            const int src = j & 31;
-            const int32_t a = __shfl_sync(0xffffffffu, kp, src);
-            const int32_t m = __shfl_sync(0xffffffffu, kc, src);
-            const int32_t n = __shfl_sync(0xffffffffu, kn, src);
-            const int32_t k = j < 32 ? a : j < 64 ? m : n;
-            if (d < len && j != 32 + lane) rank += k < kc;
+        if (__all_sync(0xffffffffu, !fast || (s >= 32 && e <= 64))) {
+            // every run of this block lies inside it: rank within this block's keys
+            for (int d = 0; d < maxlen; ++d) {
+                const int j = s + d;
+                const int32_t k = __shfl_sync(0xffffffffu, kc, j & 31);
+                if (d < len && j != 32 + lane) rank += k < kc;
+            }
+        } else {
+            for (int d = 0; d < maxlen; ++d) {
+                const int j = s + d;
+                const int src = j & 31;
+                const int32_t a = __shfl_sync(0xffffffffu, kp, src);
+                const int32_t m = __shfl_sync(0xffffffffu, kc, src);
+                const int32_t n = __shfl_sync(0xffffffffu, kn, src);
+                const int32_t k = j < 32 ? a : j < 64 ? m : n;
+                if (d < len && j != 32 + lane) rank += k < kc;
+            }
         }
         if (write && kc != 0) {
             int64_t pos;
