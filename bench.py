@@ -30,15 +30,15 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-from thunderrw_gb300 import replicas  # noqa: E402
+from thunderrw_gb300 import bytes_model, replicas  # noqa: E402
 
 BYTES_PER_STEP = {
     # Algorithmic bytes per move (32-byte sectors of each independent random
-    # access, 4 bytes per path entry): row pair 32 + adjacency entry 32 +
-    # visit-count update 32.
-    "ppr": 96,
+    # access, 4 bytes per path entry), thunderrw_gb300/bytes_model.py:
+    # row pair 32 + adjacency entry 32 + visit-count update 32.
+    "ppr": bytes_model.UNIFORM_PPR,
     # row pair 32 + alias slot 32 + path entry 4
-    "deepwalk": 68,
+    "deepwalk": bytes_model.STATIC_ALIAS,
 }
 
 WORKLOADS = {
@@ -481,15 +481,13 @@ def run_ours(args):
     if args.workload in BYTES_PER_STEP:
         bps = BYTES_PER_STEP[args.workload]
     else:
-        # Algorithmic bytes per move from the oracle's sector-counting pass
-        # over the first 4096 walkers of this workload (same seeds).
-        from oracle import oracle as O
-        og = O.Graph(inp["row"], inp["adj"], inp["weight"], inp.get("label"))
-        d = O.make_desc(args.workload, app.mode, app.sampler, length=wl["length"], p=wl.get("p", 1.0),
-                        q=wl.get("q", 1.0), schema=wl.get("schema"), seed=2000)
-        nb, ns = O.count_bytes(og, d, src[:4096].cpu().numpy(), record_paths=True)
-        bps = nb / max(1, ns)
-        del og
+        # Algorithmic bytes per move of the timed walks (the last batch's
+        # paths, first 65536 walkers) under the kernel's own access pattern.
+        sample = paths[:65536].cpu().numpy()
+        if args.workload == "node2vec":
+            bps = bytes_model.node2vec(sample, wl["length"])
+        else:
+            bps = bytes_model.metapath(sample, inp["row"].cpu().numpy(), wl["length"])
     achieved = steps_per_batch * bps / kmean / 1e9
     peaks = {}
     try:

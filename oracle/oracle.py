@@ -63,6 +63,8 @@ def lib():
                                   ctypes.c_int32, P, P, P, ctypes.c_int32]
         L.oracle_walk_interleaved.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, P,
                                               ctypes.c_int32, P, P, P, ctypes.c_int32, ctypes.c_int32]
+        L.oracle_set_neighbor_accounting.argtypes = [ctypes.c_int32]
+        L.oracle_set_neighbor_accounting.restype = None
         L.oracle_count_bytes.argtypes = [P, P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_int32, ctypes.c_int32, P, P, ctypes.c_int32]
         _lib = L
@@ -167,7 +169,12 @@ def walk(graph: Graph, desc, sources, per_query=0, id_base=0, path_cap=0, want_l
 
 
 def count_bytes(graph: Graph, desc, sources, per_query=0, id_base=0, record_paths=True,
-                count_visits=False, threads=0):
+                count_visits=False, threads=0, neighbor_probe=False):
+    """Algorithmic bytes (32-byte sectors per independent access) and steps
+    of the walks.  ``neighbor_probe`` charges Node2Vec's neighbour test as one
+    hash probe (the GPU engine on a symmetric graph) instead of the
+    reference's binary search."""
+    lib().oracle_set_neighbor_accounting(1 if neighbor_probe else 0)
     src = as_np(sources, np.int32)
     W = src.size * per_query if per_query > 0 else src.size
     nbytes = ctypes.c_uint64(0)

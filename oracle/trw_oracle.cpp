@@ -163,6 +163,13 @@ struct Scratch {
     std::vector<int32_t> small, large;
 };
 
+/* How oracle_count_bytes charges Node2Vec's neighbour test: 0 = the
+ * reference's binary search (graph.h:180-199), 1 = one 32-byte probe of a
+ * hash set of the edges (the GPU engine's method on symmetric graphs). */
+static std::atomic<int> g_neighbor_accounting{0};
+
+extern "C" void oracle_set_neighbor_accounting(int32_t kind) { g_neighbor_accounting.store(kind); }
+
 /* Sector accounting for oracle_count_bytes. */
 struct ByteCounter {
     uint64_t bytes = 0;
@@ -254,7 +261,10 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
                 r = real2(c.u32()) * maxw;
                 if (kCount) {
                     bc->touch(g->adj + off + p0);
-                    if (app.kind == APP_NODE2VEC && w.len != 1 && nb != w.prev) {
+                    if (app.kind == APP_NODE2VEC && w.len != 1 && nb != w.prev &&
+                        g_neighbor_accounting.load(std::memory_order_relaxed) == 1) {
+                        bc->bytes += 32;  /* one probe of a hash set of the edges */
+                    } else if (app.kind == APP_NODE2VEC && w.len != 1 && nb != w.prev) {
                         int32_t u = w.prev, v = nb;
                         bc->touch(g->row + u); bc->touch(g->row + v);
                         int64_t du = g->row[u + 1] - g->row[u], dv = g->row[v + 1] - g->row[v];

@@ -104,6 +104,10 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
  * distinct 32-byte sectors of each independent random access, the sectors
  * spanned by contiguous row scans, 4 bytes per path write and one 32-byte
  * sector per visit-count update.  Returns total bytes in *bytes. */
+/* Node2Vec neighbour-test accounting of oracle_count_bytes: 0 = binary
+ * search (default), 1 = one 32-byte hash probe. */
+void oracle_set_neighbor_accounting(int32_t kind);
+
 int oracle_count_bytes(const oracle_graph *g, const oracle_walk_desc *d,
                        const int32_t *sources, int64_t num_walkers, int64_t per_query,
                        int64_t id_base, int32_t record_paths, int32_t count_visits,

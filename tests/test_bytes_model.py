@@ -1,0 +1,63 @@
+"""The roofline's byte model (thunderrw_gb300/bytes_model.py) against the
+oracle's sector-counting pass over the same walks."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from thunderrw_gb300 import bytes_model as B
+from thunderrw_gb300 import generators as G
+
+
+def _aligned(a, dtype):
+    """A copy of `a` whose data starts on a 64-byte boundary (sector
+    accounting depends on it)."""
+    a = np.asarray(a, dtype=dtype)
+    buf = np.empty(a.nbytes + 64, dtype=np.uint8)
+    off = (-buf.ctypes.data) % 64
+    out = buf[off:off + a.nbytes].view(dtype)
+    out[...] = a
+    return out
+
+
+@pytest.fixture(scope="module")
+def graph():
+    g = G.make_graph("rmat", 1 << 11, 10, seed=31, labels=3)
+    return O.Graph(_aligned(g["row"], np.int64), _aligned(g["adj"], np.int32), _aligned(g["weight"], np.float64),
+                   _aligned(g["label"], np.int32))
+
+
+def test_node2vec_model_equals_probe_accounting(graph):
+    src = np.nonzero(np.diff(graph.row))[0][:1500].astype(np.int32)
+    d = O.make_desc("node2vec", "dynamic", "maxweight_rejection", length=12, p=1.0, q=1.0, seed=3)  # no rejections
+    walks = O.walk(graph, d, src, path_cap=12)
+    nb, ns = O.count_bytes(graph, d, src, record_paths=True, neighbor_probe=True)
+    assert ns == walks["steps"]
+    assert B.node2vec(walks["paths"], 12) == pytest.approx(nb / ns, rel=1e-12)
+    # with rejections (p = 2, q = 0.5) the model charges accepted moves only: a lower bound
+    d2 = O.make_desc("node2vec", "dynamic", "maxweight_rejection", length=12, p=2.0, q=0.5, seed=3)
+    w2 = O.walk(graph, d2, src, path_cap=12)
+    nb2, ns2 = O.count_bytes(graph, d2, src, record_paths=True, neighbor_probe=True)
+    assert B.node2vec(w2["paths"], 12) <= nb2 / ns2
+    # the reference's binary search costs more than one probe
+    nb3, _ = O.count_bytes(graph, d2, src, record_paths=True, neighbor_probe=False)
+    assert nb3 > nb2
+
+
+def test_metapath_model_equals_oracle(graph):
+    src = np.nonzero(np.diff(graph.row))[0][:1500].astype(np.int32)
+    d = O.make_desc("metapath", "dynamic", "its", length=10, schema=[0, 1, 2], seed=4)
+    walks = O.walk(graph, d, src, path_cap=10)
+    nb, ns = O.count_bytes(graph, d, src, record_paths=True)
+    assert (walks["lengths"] < 10).any()  # some walks stop on rows without the label
+    assert B.metapath(walks["paths"], graph.row, 10) == pytest.approx(nb / ns, rel=1e-12)
+
+
+def test_constant_models(graph):
+    src = np.nonzero(np.diff(graph.row))[0][:800].astype(np.int32)
+    graph.build_tables("alias", 0)
+    d = O.make_desc("deepwalk", "static", "alias", length=10, seed=5)
+    nb, ns = O.count_bytes(graph, d, src, record_paths=True)
+    assert nb / ns == B.STATIC_ALIAS
+    d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=6)
+    nb, ns = O.count_bytes(graph, d, src, per_query=20, record_paths=False, count_visits=True)
+    assert nb / ns == B.UNIFORM_PPR
