@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--scale", type=int, default=None, help="override log2(N) (small runs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-tune", action="store_true", help="keep the automatic launch shape (no autotuning)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--dense", action="store_true", help="PPR: dense Q x N count output instead of sparse CSR")
     return ap.parse_args()
@@ -341,6 +342,20 @@ def run_ours(args):
                                ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
                                ctypes.c_void_p(stream.cuda_stream)))
 
+    # ---- launch shape: tuned once on a sample of this workload, as a user
+    # would (thunderrw_gb300/autotune.py), outside every timed region
+    shape = None
+    if not args.no_tune:
+        from thunderrw_gb300 import autotune
+        if args.workload == "ppr":
+            res = autotune.tune(graph, E.PPR(wl["tp"]), src, walkers_per_query=per_q, rings=(1, 2), ctas=(0, 4),
+                                repeats=2)
+        else:
+            res = autotune.tune(graph, app, src, rings=(1, 2, 4), ctas=(0, 2, 4), repeats=2)
+        shape = {"slot": res.sampler, "walkers_per_lane": res.best[0], "ctas_per_sm": res.best[1],
+                 "tuned_on_walkers": res.walkers, "candidates": len(res.timings)}
+        torch.cuda.synchronize()
+
     # ---- warm-up
     for i in range(args.warmup):
         one_step(1000 + i)
@@ -530,6 +545,7 @@ def run_ours(args):
             "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": workload_name(wl, args), "n": graph.n, "e": graph.e,
                        "steps_per_batch": steps_per_batch, "engine": "persistent",
+                       "launch_shape": shape or "automatic (0 = automatic)",
                        "counts": ("dense int32 [Q][N], zeroed every step" if args.workload == "ppr" and not sparse
                                   else "sparse CSR per query (offsets, vertex, int32 count)")
                        if args.workload == "ppr" else None,
