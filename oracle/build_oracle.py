@@ -1,4 +1,4 @@
-"""Build recipe for the CPU checkers (test infrastructure only).
+"""Build recipe for the CPU oracle and reference harness (test infrastructure only).
 
 * ``oracle/liboracle.so``: the C++ restatement of the reference path
   (trw_oracle.cpp), compiled with ``-ffp-contract=off``.
@@ -51,7 +51,7 @@ def ref_cmds(reference_root):
 
 def ref_tool_cmds(reference_root):
     """The reference's EdgeList2CSR tool (toolset/edgelist_to_csr.cpp over
-    util/graph/graph.cpp), the checker of thunderrw_gb300/toolset.py."""
+    util/graph/graph.cpp), the oracle of thunderrw_gb300/toolset.py."""
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     return [["g++", "-O2", "-std=c++14", "-include", "cstdint", "-w", "-I", reference_root,

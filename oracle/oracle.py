@@ -1,4 +1,4 @@
-"""ctypes front end of the CPU checker -- TEST INFRASTRUCTURE ONLY.
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 Loaded by tests/, ``__graft_entry__.smoke()`` and the cpu_baseline/reference
 legs of bench.py.  The product library never imports this module.

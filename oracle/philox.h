@@ -2,7 +2,7 @@
  * philox.h -- TEST INFRASTRUCTURE ONLY.
  *
  * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
- * easy as 1, 2, 3", SC'11) for the CPU checkers.  Each round multiplies
+ * easy as 1, 2, 3", SC'11) for the CPU oracle.  Each round multiplies
  * counter words 0 and 2 by the two Philox multipliers (32x32 -> 64 bits) and
  * emits (hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0); the key is bumped by the two
  * Weyl constants between rounds.

@@ -1,5 +1,5 @@
 /*
- * trw_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the checker, never the product).
+ * trw_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle, never the product).
  *
  * CPU restatement of ThunderRW's sampling path.  Each function names the
  * reference lines it follows (paths relative to the ThunderRW tree).  Built

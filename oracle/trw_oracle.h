@@ -1,8 +1,8 @@
 /*
  * trw_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
- * CPU restatement of ThunderRW's Gather-Move-Update walk path, used as the
- * checker for the GPU engine.  Only tests/, __graft_entry__.smoke() and the
+ * CPU restatement of ThunderRW's Gather-Move-Update walk path, the oracle
+ * the GPU engine is tested against.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference legs of bench.py may load it.  The product path
  * (libtrw_gpu.so) never links or calls anything here.
  *

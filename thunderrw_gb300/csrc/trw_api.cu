@@ -499,7 +499,7 @@ int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *w
     if (!out) return fail(TRW_ERR_INVALID, "out is null");
     *out = nullptr;
     if (n <= 0 || e < 0 || !row_ptr || (e > 0 && !adj)) return fail(TRW_ERR_INVALID, "bad CSR arguments");
-    if (e >= (int64_t)1 << 31) return fail(TRW_ERR_CAPACITY, "e = %lld: this build stores int32 row offsets (e < 2^31)",
+    if (e >= (int64_t)1 << 31) return fail(TRW_ERR_CAPACITY, "e = %lld: the library stores int32 row offsets (e < 2^31)",
                                            (long long)e);
     trw_graph *g = new trw_graph();
     auto bail = [&](int code) { destroy_graph(g); return code; };
