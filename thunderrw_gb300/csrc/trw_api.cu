@@ -100,6 +100,10 @@ struct trw_graph {
     // 1 = built, -1 = no room for it (the walks then binary-search the lists)
     unsigned long long *edges = nullptr;
     int32_t edge_bits = 0;
+    // rows longer than 32 entries, longest first (the warp table builders'
+    // work list); n_long < 0 until first needed
+    int32_t *long_rows = nullptr;
+    int32_t n_long = -1;
     int32_t edge_symmetric = 0;
     int edge_state = 0;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
@@ -142,6 +146,7 @@ void destroy_graph(trw_graph *g) {
     if (!g) return;
     cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state); cudaFree(g->edges);
+    cudaFree(g->long_rows);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
@@ -201,6 +206,35 @@ int build_edge_set(trw_graph *g, cudaStream_t st) {
     return TRW_OK;
 }
 
+// The rows the warp builders take (longer than 32 entries), longest first:
+// each gets a warp of its own block, so the hub rows -- whose alias pairing
+// and prefix chains are sequential double arithmetic -- start first and
+// run on different SMs instead of sharing one CTA.
+int collect_long_rows(trw_graph *g, cudaStream_t st) {
+    int2 *d_list = nullptr;
+    int *d_count = nullptr;
+    TRW_CUDA(cudaMalloc(&d_list, sizeof(int2) * (size_t)g->n));
+    TRW_CUDA(cudaMalloc(&d_count, sizeof(int)));
+    TRW_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), st));
+    TRW_CUDA(launch_collect_long_rows(dev_view(g), d_list, d_count, st));
+    int count = 0;
+    TRW_CUDA(cudaMemcpyAsync(&count, d_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    std::vector<int2> list((size_t)count);
+    if (count) TRW_CUDA(cudaMemcpy(list.data(), d_list, sizeof(int2) * (size_t)count, cudaMemcpyDeviceToHost));
+    cudaFree(d_list);
+    cudaFree(d_count);
+    std::sort(list.begin(), list.end(), [](const int2 &a, const int2 &b) { return a.x != b.x ? a.x > b.x : a.y < b.y; });
+    std::vector<int32_t> ids((size_t)count);
+    for (int i = 0; i < count; ++i) ids[(size_t)i] = list[(size_t)i].y;
+    if (count) {
+        TRW_CUDA(cudaMalloc(&g->long_rows, sizeof(int32_t) * (size_t)count));
+        TRW_CUDA(cudaMemcpy(g->long_rows, ids.data(), sizeof(int32_t) * (size_t)count, cudaMemcpyHostToDevice));
+    }
+    g->n_long = count;
+    return TRW_OK;
+}
+
 int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
     const DevGraph d = dev_view(g);
     if (kind == TRW_WEIGHTS_EDGE && !g->weight) return fail(TRW_ERR_INVALID, "edge weights were not supplied");
@@ -209,13 +243,17 @@ int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
     if ((sampler == TRW_SAMPLER_ALIAS && g->alias) || (sampler == TRW_SAMPLER_ITS && g->prefix) ||
         (sampler == TRW_SAMPLER_REJECTION && g->rmax))
         TRW_CUDA(cudaDeviceSynchronize());
+    if ((sampler == TRW_SAMPLER_ALIAS || sampler == TRW_SAMPLER_ITS) && g->n_long < 0) {
+        int rc = collect_long_rows(g, st);
+        if (rc) return rc;
+    }
     if (sampler == TRW_SAMPLER_ALIAS) {
         if (!g->alias) TRW_CUDA(cudaMalloc(&g->alias, sizeof(AliasSlot) * (size_t)(g->e ? g->e : 1)));
-        TRW_CUDA(launch_build_alias(d, unit, g->alias, st));
+        TRW_CUDA(launch_build_alias(d, unit, g->alias, g->long_rows, g->n_long, st));
         g->alias_kind = kind;
     } else if (sampler == TRW_SAMPLER_ITS) {
         if (!g->prefix) TRW_CUDA(cudaMalloc(&g->prefix, sizeof(double) * (size_t)(g->e ? g->e : 1)));
-        TRW_CUDA(launch_build_prefix(d, unit, g->prefix, st));
+        TRW_CUDA(launch_build_prefix(d, unit, g->prefix, g->long_rows, g->n_long, st));
         g->prefix_kind = kind;
     } else if (sampler == TRW_SAMPLER_REJECTION) {
         if (!g->rmax) TRW_CUDA(cudaMalloc(&g->rmax, sizeof(double) * (size_t)g->n));

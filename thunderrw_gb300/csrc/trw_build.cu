@@ -117,10 +117,9 @@ __device__ __forceinline__ double warp_row_sum(const DevGraph &g, int unit, int2
 
 // its_initialization for a long row: the same left-to-right chain; lane k
 // keeps the value after adding entry k of the block and stores it (coalesced).
-__global__ void build_prefix_warp_kernel(const DevGraph g, int unit, double *out) {
-    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void build_prefix_warp_kernel(const DevGraph g, int unit, double *out, const int32_t *long_rows) {
+    const int32_t v = long_rows[blockIdx.x];  // one warp per block: long rows spread over the SMs
     const int lane = threadIdx.x & 31;
-    if (v >= g.n) return;
     const int2 r = __ldg(g.rows + v);
     if (r.y - r.x <= kWarpRow) return;
     double acc = 0.0;
@@ -145,10 +144,9 @@ __global__ void build_prefix_warp_kernel(const DevGraph g, int unit, double *out
 // lockstep by the warp with 32-entry register blocks of the small queue and
 // of the large list; table entries hold neighbour indices until a final
 // parallel pass maps them to vertex ids.
-__global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *out) {
-    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *out, const int32_t *long_rows) {
+    const int32_t v = long_rows[blockIdx.x];  // one warp per block: long rows spread over the SMs
     const int lane = threadIdx.x & 31;
-    if (v >= g.n) return;
     const int2 r = __ldg(g.rows + v);
     const int32_t d = r.y - r.x;
     if (d <= kWarpRow) return;
@@ -184,7 +182,7 @@ __global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *o
     // pairing loop (alias_sampling.h:29-39) in lockstep
     const int32_t nl = d - ns;
     int32_t sp = 0, c = 0;
-    int32_t sblk = -1, svalid = 0, lblk = -1;
+    int32_t sblk = -1, lblk = -1;
     double s_prob = 0.0, l_prob = 0.0;
     int32_t s_idx = 0, l_idx = 0;
     auto load_l = [&](int32_t pos) {  // large list entries are untouched until stashed
@@ -195,12 +193,12 @@ __global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *o
     if (nl) load_l(ns);
     double vl = __shfl_sync(kFull, l_prob, 0);
     while (sp < ns + c && c < nl) {
-        // small queue head: slot sp; slots >= ns hold larges whose final value
-        // was stashed there, so a cached block is only valid below ns + c at load
-        if (sblk < 0 || sp >= sblk + 32 || sp >= svalid) {
+        // small queue head: slot sp.  Slots >= ns hold larges, whose value
+        // changes when they turn small; the cached block is kept in step with
+        // those changes below, so it is reloaded only every 32 smalls.
+        if (sblk < 0 || sp >= sblk + 32) {
             __syncwarp();
             sblk = sp;
-            svalid = ns + c;
             const int32_t j = sp + lane;
             if (j < d) { s_prob = tab[j].prob; s_idx = tab[j].first; }
         }
@@ -212,6 +210,7 @@ __global__ void build_alias_warp_kernel(const DevGraph g, int unit, AliasSlot *o
         vl = vl + vs - 1;  // src[large] + src[small] - 1
         if (vl < 1) {
             if (lane == 0) tab[ns + c].prob = vl;
+            if (lane == ns + c - sblk) s_prob = vl;  // the cached copy of slot ns + c, if cached
             ++c;
             if (c < nl) {
                 if (ns + c >= lblk + 32) { __syncwarp(); load_l(ns + c); }
@@ -281,6 +280,14 @@ __global__ void validate_kernel(const int64_t *row, const int32_t *adj, int32_t 
 
 inline unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
 
+// (degree, vertex) of every row longer than kWarpRow, appended in any order.
+__global__ void collect_long_rows_kernel(const DevGraph g, int2 *list, int *count) {
+    const int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.n) return;
+    const int2 r = __ldg(g.rows + v);
+    if (r.y - r.x > kWarpRow) list[atomicAdd(count, 1)] = make_int2(r.y - r.x, v);
+}
+
 constexpr int kEdgeRun = 8;  // consecutive CSR entries per thread in the edge-set kernels
 
 // Source vertex of CSR entry i: the largest v with rows[v].x <= i (rows of
@@ -335,17 +342,25 @@ __global__ void edge_symmetry_kernel(DevGraph g, int *symmetric) {
 
 }  // namespace
 
-cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st) {
+cudaError_t launch_collect_long_rows(const DevGraph &g, int2 *list, int *count, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
-    build_alias_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
-    build_alias_warp_kernel<<<blocks_for((int64_t)g.n * 32), 256, 0, st>>>(g, unit, out);
+    collect_long_rows_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, list, count);
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st) {
+cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, const int32_t *long_rows,
+                               int32_t n_long, cudaStream_t st) {
+    if (g.n <= 0) return cudaSuccess;
+    build_alias_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    if (n_long > 0) build_alias_warp_kernel<<<(unsigned)n_long, 32, 0, st>>>(g, unit, out, long_rows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, const int32_t *long_rows,
+                                int32_t n_long, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_prefix_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
-    build_prefix_warp_kernel<<<blocks_for((int64_t)g.n * 32), 256, 0, st>>>(g, unit, out);
+    if (n_long > 0) build_prefix_warp_kernel<<<(unsigned)n_long, 32, 0, st>>>(g, unit, out, long_rows);
     return cudaGetLastError();
 }
 

@@ -38,12 +38,17 @@ cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int
 // *out = parts[0] + ... + parts[n-1], on the device
 cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st);
 
-cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, cudaStream_t st);
+// (degree, vertex) of the rows the warp builders take, appended in any order
+cudaError_t launch_collect_long_rows(const DevGraph &g, int2 *list, int *count, cudaStream_t st);
+// long_rows: the vertices of rows longer than 32 entries (longest first), one warp each
+cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, const int32_t *long_rows,
+                               int32_t n_long, cudaStream_t st);
 // Node2Vec's edge set: `set` (2^bits slots) must hold kEdgeEmpty everywhere;
 // *symmetric must hold 1 and is cleared if some edge's reverse is missing.
 cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, int32_t bits, int *symmetric,
                                   cudaStream_t st);
-cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, cudaStream_t st);
+cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, const int32_t *long_rows,
+                                int32_t n_long, cudaStream_t st);
 cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st);
 cudaError_t launch_validate_graph(const int64_t *row, const int32_t *adj, int32_t n, int64_t e, int check_sorted,
                                   int2 *rows_out, int *bad, int *max_degree, cudaStream_t st);
