@@ -170,16 +170,18 @@ struct WalkParams {
     int64_t alias_scratch_stride;
     // sparse visit counts: per query an open-addressing table of 2^table_bits
     // slots stored as 2^table_bits keys (vertex + 1, 0 = empty) followed by
-    // 2^table_bits counts.  Keys and counts live in separate sectors so that
-    // reading a hot key never queues behind the atomic adds to its count.
+    // 2^table_bits counts (visits minus one).  Keys and counts live in
+    // separate sectors so that reading a hot key never queues behind the
+    // atomic adds to its count.
     int32_t *table;
     int32_t table_bits;
 };
 
 // Adds `inc` visits of vertex v to a query's table t (keys t[0..C), counts
-// t[C..2C)): linear probing on key v + 1, 0 = empty.  Which slots end up occupied does not depend on
-// the insertion order; only the order of keys inside a run of occupied
-// slots does.
+// t[C..2C)): linear probing on key v + 1, 0 = empty.  A slot's count holds
+// its visits minus one: the CAS that claims the slot stands for the first.
+// Which slots end up occupied does not depend on the insertion order; only
+// the order of keys inside a run of occupied slots does.
 __device__ __forceinline__ void table_add(int32_t *t, int32_t bits, int32_t v, int inc, int *error) {
     const uint32_t mask = (1u << bits) - 1u;
     uint32_t h = ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
@@ -187,8 +189,11 @@ __device__ __forceinline__ void table_add(int32_t *t, int32_t bits, int32_t v, i
     for (uint32_t probe = 0; probe <= mask; ++probe) {
         int k = __ldcg(t + h);
         if (k == 0) {
-            const int old = atomicCAS(t + h, 0, key);
-            k = old == 0 ? key : old;
+            k = atomicCAS(t + h, 0, key);
+            if (k == 0) {  // claimed
+                if (inc > 1) atomicAdd(t + mask + 1 + h, inc - 1);
+                return;
+            }
         }
         if (k == key) { atomicAdd(t + mask + 1 + h, inc); return; }
         h = (h + 1) & mask;

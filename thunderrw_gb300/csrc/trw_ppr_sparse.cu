@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
                 pos = before - head - back + rank;
             }
             vout[pos] = kc - 1;
-            cout[pos] = cc;
+            cout[pos] = cc + 1;  // the table counts visits after the first
         }
         kp = kc; op = oc;
         kc = kn; cc = cn;

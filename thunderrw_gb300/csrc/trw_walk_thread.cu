@@ -73,12 +73,15 @@ __device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
 //    vertex's home slot;
 //  * at round i+1, right after the row-pair loads are issued, the load result
 //    is consumed: our key -> add the count (fire-and-forget); empty -> claim
-//    it with a CAS and add the count speculatively; another key -> load the
-//    next slot (linear probing, as table_add);
+//    it with a CAS, adding all but one of the visits speculatively (a slot's
+//    count holds its visits minus the first, which its claim implies; for a
+//    single visit, the common case, the claim is the only atomic); another
+//    key -> load the next slot (linear probing, as table_add);
 //  * the CAS result is consumed when the slot records its next visit, a whole
-//    dependent-load chain later: only a lost race to another key matters; it
-//    takes the speculative count back and probes on.  (Each query's number of
-//    distinct vertices is counted from its table after the walk.)
+//    dependent-load chain later: a race lost to the same vertex adds the one
+//    visit the claim would have implied; one lost to another vertex takes the
+//    speculative part back and probes on.  (Each query's number of distinct
+//    vertices is counted from its table after the walk.)
 struct PendingInsert {
     int32_t q;      // query of the table, -1 = nothing pending
     uint32_t h;     // slot being examined
@@ -104,8 +107,13 @@ __device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, 
     int32_t *t = table_of(p, pi.q);
     for (;;) {
         if (pi.cas) {
-            if (pi.old == 0 || pi.old == pi.key) { pi.q = -1; return; }  // the slot holds our key
-            atomicAdd(t + mask + 1 + pi.h, -pi.inc);                       // lost it to another vertex
+            if (pi.old == 0) { pi.q = -1; return; }  // claimed: its first visit is implied
+            if (pi.old == pi.key) {                  // another warp claimed it for this vertex
+                atomicAdd(t + mask + 1 + pi.h, 1);
+                pi.q = -1;
+                return;
+            }
+            if (pi.inc > 1) atomicAdd(t + mask + 1 + pi.h, 1 - pi.inc);  // lost it to another vertex
         } else {
             if (pi.old == pi.key) {
                 atomicAdd(t + mask + 1 + pi.h, pi.inc);
@@ -114,7 +122,7 @@ __device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, 
             }
             if (pi.old == 0) {
                 pi.old = atomicCAS(t + pi.h, 0, pi.key);
-                atomicAdd(t + mask + 1 + pi.h, pi.inc);
+                if (pi.inc > 1) atomicAdd(t + mask + 1 + pi.h, pi.inc - 1);  // speculative
                 pi.cas = 1;
                 if (!blocking) return;
                 continue;
