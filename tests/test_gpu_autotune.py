@@ -19,14 +19,17 @@ def test_tune_sets_fastest_shape_and_keeps_results():
         app = E.DeepWalk(12)
         before = E.compute(graph, src, app, seed=5)
         res = autotune.tune(graph, app, src, rings=(1, 4), ctas=(0, 2), repeats=1)
-        assert set(res.timings) == {(1, 0), (1, 2), (4, 0), (4, 2)}
-        assert res.best == min(res.timings, key=res.timings.get)
+        assert set(res.timings) == {(0, 0), (1, 0), (1, 2), (4, 0), (4, 2)}
+        fastest = min(res.timings, key=res.timings.get)
+        # the automatic shape stays unless beaten by more than 3 %
+        assert res.best in (fastest, (0, 0))
+        assert res.timings[res.best] <= res.timings[fastest] * 1.03 + 1e-9
         assert graph.engine_shape("alias") == res.best
         after = E.compute(graph, src, app, seed=5)
         assert torch.equal(before.paths, after.paths) and before.steps == after.steps
         # sparse PPR tunes the uniform slot; dynamic ITS (warp family) only CTAs
         r2 = autotune.tune(graph, E.PPR(0.2), src[:8], walkers_per_query=2000, rings=(1, 2), ctas=(0,), repeats=1)
-        assert r2.sampler == "uniform" and set(r2.timings) == {(1, 0), (2, 0)}
+        assert r2.sampler == "uniform" and set(r2.timings) == {(0, 0), (1, 0), (2, 0)}
         r3 = autotune.tune(graph, E.DeepWalk(6, mode="dynamic", sampler="its"), src, ctas=(0, 1), repeats=1)
         assert r3.sampler == "its" and set(r3.timings) == {(0, 0), (0, 1)}
         assert np.isfinite(list(r3.timings.values())).all()

@@ -4,9 +4,10 @@ The reference fixes its ring (RING_SIZE = 64 slots per thread, 32 search
 frames, creeper.h / types.h) at compile time.  Here the equivalent knobs are
 runtime launch shapes of the persistent engine: walkers in flight per lane
 (the ring depth R, 1/2/4/8) and CTAs per SM.  Which shape is fastest depends
-on the graph's degree profile and the app: sparse-table PPR wants R = 1
-(its insert records cost registers), max-weight rejection R = 2, static alias
-R = 4 on large batches.  `tune` times each candidate shape on a sample of the
+on the graph's degree profile and the app: sparse-table PPR and max-weight
+rejection want R = 1, static alias R = 4 on large batches, and a batch of
+about one walker per lane (DeepWalk on Chung-Lu 2^18) runs fastest with 4
+CTAs per SM instead of the 6 that fit.  `tune` times each candidate shape on a sample of the
 caller's own workload with CUDA events and sets the fastest on the graph
 (`trw_set_engine_shape`), so later calls with the same sampler use it.
 Walks are a function of (seed, walker, step) only, so the shape never changes
@@ -44,12 +45,15 @@ def _slot(app: E.App, mode: Optional[str], sampler: Optional[str]) -> Tuple[str,
 def tune(graph: E.Graph, app: E.App, sources, walkers_per_query: int = 0, mode: Optional[str] = None,
          sampler: Optional[str] = None, rings: Sequence[int] = (1, 2, 4, 8),
          ctas: Sequence[int] = (0, 2, 4, 8), sample_walkers: Optional[int] = None, repeats: int = 3,
-         record_paths: bool = True, seed: int = 12345, apply: bool = True) -> TuneResult:
+         record_paths: bool = True, seed: int = 12345, apply: bool = True,
+         tolerance: float = 0.03) -> TuneResult:
     """Times every (ring, CTAs/SM) candidate on a sample of the workload and
     keeps the fastest.  `walkers_per_query` > 0 tunes sparse batched PPR
     (`sources` are then the queries).  The sample keeps at least 16 walkers
     per lane of the GPU (the engine's steady state), or the whole workload
-    if it is smaller."""
+    if it is smaller.  The automatic shape (0, 0) is timed too and kept
+    unless a candidate beats it by more than `tolerance`, so timing noise
+    does not move the shape."""
     dev = graph.device
     src = torch.as_tensor(sources).to(device=dev, dtype=torch.int32).flatten()
     slot, warp_family = _slot(app, mode, sampler)
@@ -63,10 +67,11 @@ def tune(graph: E.Graph, app: E.App, sources, walkers_per_query: int = 0, mode: 
     else:
         src = src[:min(src.numel(), target)]
         walkers = src.numel()
-    cands: List[Tuple[int, int]] = []
+    cands: List[Tuple[int, int]] = [(0, 0)]
     for r in ((0,) if warp_family else rings):
         for c in ctas:
-            cands.append((r, c))
+            if (r, c) not in cands:
+                cands.append((r, c))
     old = graph.engine_shape(slot)
     stream = torch.cuda.current_stream(dev)
 
@@ -93,6 +98,8 @@ def tune(graph: E.Graph, app: E.App, sources, walkers_per_query: int = 0, mode: 
     finally:
         graph.set_engine_shape(slot, *old)
     best = min(timings, key=timings.get)
+    if timings[(0, 0)] <= timings[best] * (1.0 + tolerance):
+        best = (0, 0)
     if apply:
         graph.set_engine_shape(slot, *best)
     return TuneResult(slot, best, timings[best], timings, walkers)
