@@ -501,6 +501,8 @@ def run_ours(args):
         sample = paths[:65536].cpu().numpy()
         if args.workload == "node2vec":
             bps = bytes_model.node2vec(sample, wl["length"])
+        elif graph.indexes()[1] == 1:  # MetaPath answered from the label index
+            bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"])
         else:
             bps = bytes_model.metapath(sample, inp["row"].cpu().numpy(), wl["length"])
     achieved = steps_per_batch * bps / kmean / 1e9

@@ -126,6 +126,17 @@ int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degr
  * only when done; asynchronous callers use this as the join point). */
 int trw_graph_synchronize(trw_graph *g);
 
+/* Which lookup structures the graph's walks use (no counterpart in the
+ * reference; each replaces a per-step search with a lookup and is built by
+ * the first walk that needs it): the Node2Vec edge set (replacing
+ * Graph::is_neighbor's binary search, graph.h:180-199) and the MetaPath
+ * label index (replacing dynamic ITS's scan of the label row,
+ * inverse_transformation_sampling.h:288-313).  Each state: 0 = not built
+ * yet, 1 = built, -1 = not applicable (MetaPath labels outside [0, 64)) or
+ * no room on the device; the walks then keep the searches.  Results are the
+ * same either way. */
+int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *label_index_state);
+
 /* ---- static tables ---------------------------------------------------- */
 
 /* Replaces static_initialization (creeper.h:102-175) and the offline

@@ -169,12 +169,13 @@ def walk(graph: Graph, desc, sources, per_query=0, id_base=0, path_cap=0, want_l
 
 
 def count_bytes(graph: Graph, desc, sources, per_query=0, id_base=0, record_paths=True,
-                count_visits=False, threads=0, neighbor_probe=False):
+                count_visits=False, threads=0, neighbor_probe=False, label_index=False):
     """Algorithmic bytes (32-byte sectors per independent access) and steps
     of the walks.  ``neighbor_probe`` charges Node2Vec's neighbour test as one
     hash probe (the GPU engine on a symmetric graph) instead of the
-    reference's binary search."""
-    lib().oracle_set_neighbor_accounting(1 if neighbor_probe else 0)
+    reference's binary search; ``label_index`` charges MetaPath's label scan
+    as one read of a label index's offsets."""
+    lib().oracle_set_neighbor_accounting((1 if neighbor_probe else 0) | (2 if label_index else 0))
     src = as_np(sources, np.int32)
     W = src.size * per_query if per_query > 0 else src.size
     nbytes = ctypes.c_uint64(0)

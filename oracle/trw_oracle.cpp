@@ -163,9 +163,11 @@ struct Scratch {
     std::vector<int32_t> small, large;
 };
 
-/* How oracle_count_bytes charges Node2Vec's neighbour test: 0 = the
- * reference's binary search (graph.h:180-199), 1 = one 32-byte probe of a
- * hash set of the edges (the GPU engine's method on symmetric graphs). */
+/* How oracle_count_bytes charges the searches the GPU engine replaces with
+ * lookups (bit flags; 0 = the reference's methods): 1 = Node2Vec's neighbour
+ * test as one 32-byte probe of a hash set of the edges instead of the binary
+ * search (graph.h:180-199); 2 = MetaPath's label row scan as one 32-byte read
+ * of a label index's offsets. */
 static std::atomic<int> g_neighbor_accounting{0};
 
 extern "C" void oracle_set_neighbor_accounting(int32_t kind) { g_neighbor_accounting.store(kind); }
@@ -262,7 +264,7 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
                 if (kCount) {
                     bc->touch(g->adj + off + p0);
                     if (app.kind == APP_NODE2VEC && w.len != 1 && nb != w.prev &&
-                        g_neighbor_accounting.load(std::memory_order_relaxed) == 1) {
+                        (g_neighbor_accounting.load(std::memory_order_relaxed) & 1)) {
                         bc->bytes += 32;  /* one probe of a hash set of the edges */
                     } else if (app.kind == APP_NODE2VEC && w.len != 1 && nb != w.prev) {
                         int32_t u = w.prev, v = nb;
@@ -293,7 +295,9 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
             double *wt = sc.w.data();
             for (int32_t i = 0; i < deg; ++i) wt[i] = app.weight(g, w, g->adj[off + i], off + i);
             if (kCount) {
-                if (app.kind == APP_METAPATH) bc->span(g->label + off, (size_t)deg * 4);
+                if (app.kind == APP_METAPATH && (g_neighbor_accounting.load(std::memory_order_relaxed) & 2))
+                    bc->bytes += 32;  /* the row's two label offsets of a label index */
+                else if (app.kind == APP_METAPATH) bc->span(g->label + off, (size_t)deg * 4);
                 else if (app.kind == APP_DEEPWALK || app.kind == APP_GENERIC) bc->span(g->weight + off, (size_t)deg * 8);
                 else if (app.kind == APP_NODE2VEC) bc->span(g->adj + off, (size_t)deg * 4);
             }

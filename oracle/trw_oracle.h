@@ -104,8 +104,10 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
  * distinct 32-byte sectors of each independent random access, the sectors
  * spanned by contiguous row scans, 4 bytes per path write and one 32-byte
  * sector per visit-count update.  Returns total bytes in *bytes. */
-/* Node2Vec neighbour-test accounting of oracle_count_bytes: 0 = binary
- * search (default), 1 = one 32-byte hash probe. */
+/* Accounting of oracle_count_bytes for searches the GPU engine replaces with
+ * lookups (bit flags, 0 = the reference's searches): 1 = Node2Vec's
+ * neighbour test as one 32-byte hash probe, 2 = MetaPath's label scan as one
+ * 32-byte read of label-index offsets. */
 void oracle_set_neighbor_accounting(int32_t kind);
 
 int oracle_count_bytes(const oracle_graph *g, const oracle_walk_desc *d,

@@ -52,6 +52,14 @@ def test_metapath_model_equals_oracle(graph):
     assert B.metapath(walks["paths"], graph.row, 10) == pytest.approx(nb / ns, rel=1e-12)
 
 
+def test_metapath_index_model_equals_oracle(graph):
+    src = np.nonzero(np.diff(graph.row))[0][:1500].astype(np.int32)
+    d = O.make_desc("metapath", "dynamic", "its", length=10, schema=[0, 1, 2], seed=4)
+    walks = O.walk(graph, d, src, path_cap=10)
+    nb, ns = O.count_bytes(graph, d, src, record_paths=True, label_index=True)
+    assert B.metapath_index(walks["paths"], graph.row, 10) == pytest.approx(nb / ns, rel=1e-12)
+
+
 def test_constant_models(graph):
     src = np.nonzero(np.diff(graph.row))[0][:800].astype(np.int32)
     graph.build_tables("alias", 0)

@@ -39,6 +39,8 @@ def _slot(app: E.App, mode: Optional[str], sampler: Optional[str]) -> Tuple[str,
     s = sampler or app.sampler
     if m == "uniform":
         return "uniform", False
+    if app.name == "metapath" and m == "dynamic" and s == "its":
+        return s, False  # the label index runs on the ring engine (the row scan ignores the ring)
     return s, (m == "dynamic" and s in WARP_FAMILY)
 
 

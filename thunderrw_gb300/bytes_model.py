@@ -13,7 +13,10 @@ GPU kernels' methods:
                               accepted move; rejected trials are not charged,
                               so the figure is a lower bound
   MetaPath (dynamic ITS)      row pair 32 + the label row's sectors +
-                              selected adjacency entry 32 + path 4
+                              selected adjacency entry 32 + path 4 (row scan);
+                              with the label index: row pair 32 + the two
+                              label offsets 32 + the sorted neighbour 32 +
+                              path 4
 
 The per-walk figures are computed from the paths the GPU produced, so they
 describe the same walks that were timed.
@@ -79,3 +82,16 @@ def metapath(paths: np.ndarray, row: np.ndarray, length: int) -> float:
     last = _stops(p, length)
     tail = SECTOR * last.size + int(_span_sectors(row[last] * 4, row[last + 1] * 4).sum()) * SECTOR
     return (float((SECTOR + lab + SECTOR + 4).sum()) + tail) / frm.size
+
+
+def metapath_index(paths: np.ndarray, row: np.ndarray, length: int) -> float:
+    """Bytes per move of MetaPath walks answered from the label index (a walk
+    that stops early is charged its last vertex's row pair, and its label
+    offsets when the row is not empty)."""
+    frm, to, k, p = _moves(paths)
+    if frm.size == 0:
+        return 0.0
+    row = np.asarray(row, dtype=np.int64)
+    last = _stops(p, length)
+    tail = SECTOR * last.size + SECTOR * int((row[last + 1] > row[last]).sum())
+    return (frm.size * (SECTOR * 3 + 4) + tail) / frm.size

@@ -4,6 +4,7 @@
 // state, maps the reference's (app, mode, sampler) triple (types.h:41-59,
 // creeper.h:700-788) onto the two kernel families, and stages host buffers.
 #include <algorithm>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -104,6 +105,12 @@ struct trw_graph {
     // work list); n_long < 0 until first needed
     int32_t *long_rows = nullptr;
     int32_t n_long = -1;
+    // MetaPath's label index (built by its first dynamic-ITS walk); lab_state
+    // 0 = not yet, 1 = built, -1 = labels outside [0, 64) or no room
+    int32_t *lab_nbr = nullptr;
+    int32_t *lab_off = nullptr;
+    int32_t lab_k = 0;
+    int lab_state = 0;
     int32_t edge_symmetric = 0;
     int edge_state = 0;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
@@ -146,7 +153,7 @@ void destroy_graph(trw_graph *g) {
     if (!g) return;
     cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state); cudaFree(g->edges);
-    cudaFree(g->long_rows);
+    cudaFree(g->long_rows); cudaFree(g->lab_nbr); cudaFree(g->lab_off);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
@@ -170,7 +177,47 @@ DevGraph dev_view(const trw_graph *g) {
     d.edges = g->edge_state == 1 ? g->edges : nullptr;
     d.edge_bits = g->edge_bits;
     d.edge_symmetric = g->edge_symmetric;
+    d.lab_nbr = g->lab_state == 1 ? g->lab_nbr : nullptr;
+    d.lab_off = g->lab_state == 1 ? g->lab_off : nullptr;
+    d.lab_k = g->lab_state == 1 ? g->lab_k : 0;
     return d;
+}
+
+// MetaPath's label index: each row's neighbours stably sorted by label, plus
+// per-row label offsets, so dynamic ITS over the label filter reads one entry
+// instead of scanning the row.  Only for labels in [0, 64); otherwise, or if
+// the device has no room, the walks keep scanning label rows.
+int build_label_index(trw_graph *g, cudaStream_t st) {
+    if (g->lab_state != 0 || g->e <= 0 || !g->label) return TRW_OK;
+    int *d_lh = nullptr;
+    TRW_CUDA(cudaMalloc(&d_lh, 2 * sizeof(int)));
+    const int init[2] = {INT_MAX, INT_MIN};
+    TRW_CUDA(cudaMemcpyAsync(d_lh, init, sizeof init, cudaMemcpyHostToDevice, st));
+    TRW_CUDA(launch_label_range(g->label, g->e, d_lh, st));
+    int lh[2] = {0, 0};
+    TRW_CUDA(cudaMemcpyAsync(lh, d_lh, sizeof lh, cudaMemcpyDeviceToHost, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    cudaFree(d_lh);
+    if (lh[0] < 0 || lh[1] >= kMaxIndexedLabels) { g->lab_state = -1; return TRW_OK; }
+    const int32_t K = lh[1] + 1;
+    const size_t b_off = sizeof(int32_t) * (size_t)g->n * (size_t)(K + 1);
+    const size_t b_nbr = sizeof(int32_t) * (size_t)g->e;
+    size_t free_b = 0, total_b = 0;
+    TRW_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (b_off + b_nbr + (size_t(1) << 30) > free_b || cudaMalloc(&g->lab_off, b_off) != cudaSuccess ||
+        cudaMalloc(&g->lab_nbr, b_nbr) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(g->lab_off);
+        cudaFree(g->lab_nbr);
+        g->lab_off = g->lab_nbr = nullptr;
+        g->lab_state = -1;
+        return TRW_OK;
+    }
+    TRW_CUDA(launch_build_label_index(dev_view(g), K, g->lab_off, g->lab_nbr, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    g->lab_k = K;
+    g->lab_state = 1;
+    return TRW_OK;
 }
 
 // Node2Vec's neighbour test as one hash probe instead of a binary search:
@@ -406,6 +453,16 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
         rc = build_edge_set(g, st);
         if (rc) return rc;
     }
+    if (desc->app == TRW_APP_METAPATH && pl.warp_family && pl.sampler == kITS) {
+        if (g->lab_state == 0) {
+            rc = build_label_index(g, st);
+            if (rc) return rc;
+        }
+        if (g->lab_state == 1) {  // the thread engine answers from the label index
+            pl.warp_family = false;
+            pl.sampler = kLabelIndex;
+        }
+    }
 
     // Stage host buffers.
     const bool h_src = sources && !is_device_ptr(sources);
@@ -464,7 +521,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     p.table = table;
     p.table_bits = table_bits;
 
-    LaunchShape shape = g->shape[pl.sampler];
+    LaunchShape shape = g->shape[pl.sampler == kLabelIndex ? (int)kITS : pl.sampler];
     shape.engine = engine;
     shape.num_sms = g->num_sms;
     if (shape.ring == 0) {
@@ -605,6 +662,13 @@ int trw_graph_info(const trw_graph *g, int32_t *n, int64_t *e, int32_t *max_degr
     if (n) *n = g->n;
     if (e) *e = g->e;
     if (max_degree) *max_degree = g->max_degree;
+    return TRW_OK;
+}
+
+int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *label_index_state) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    if (edge_set_state) *edge_set_state = g->edge_state;
+    if (label_index_state) *label_index_state = g->lab_state;
     return TRW_OK;
 }
 

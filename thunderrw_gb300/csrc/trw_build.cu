@@ -9,6 +9,9 @@
 // (the hubs of power-law graphs) one warp per vertex, where the warp loads
 // 32 entries at a time with coalesced loads and runs the sequential chains in
 // lockstep through shuffles.  The maximum is order-independent.
+#include <algorithm>
+#include <climits>
+
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
@@ -288,6 +291,81 @@ __global__ void collect_long_rows_kernel(const DevGraph g, int2 *list, int *coun
     if (r.y - r.x > kWarpRow) list[atomicAdd(count, 1)] = make_int2(r.y - r.x, v);
 }
 
+// Smallest and largest edge label (for the label index: every label must lie
+// in [0, kMaxIndexedLabels)).
+__global__ void label_range_kernel(const int32_t *label, int64_t e, int *lo_hi) {
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < e; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x = __ldg(label + i);
+        lo = min(lo, x);
+        hi = max(hi, x);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+        hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(lo_hi, lo);
+        atomicMax(lo_hi + 1, hi);
+    }
+}
+
+// MetaPath's label index, one warp per row (grid-stride): a stable counting
+// sort of the row's neighbours by edge label.  Lane l keeps the counts and
+// then the running output position of labels l and l + 32; each 32-entry
+// chunk is scattered label by label with ballots, lanes of one label in lane
+// order, so every label's block keeps row order.
+__global__ void build_label_index_kernel(const DevGraph g, int32_t K, int32_t *off, int32_t *nbr) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < g.n; v += warps) {
+        const int2 r = __ldg(g.rows + v);
+        int32_t c0 = 0, c1 = 0;  // counts of labels lane and lane + 32
+        for (int32_t base = r.x; base < r.y; base += 32) {
+            const int32_t i = base + lane;
+            const int32_t lab = i < r.y ? __ldg(g.label + i) : -1;
+            for (int32_t l = 0; l < K; ++l) {
+                const int32_t c = __popc(__ballot_sync(kFull, lab == l));
+                if (l == lane) c0 += c;
+                if (l == lane + 32) c1 += c;
+            }
+        }
+        // exclusive scan over labels 0..K-1 held as (lane, c0) then (lane, c1)
+        int32_t x0 = c0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(kFull, x0, o);
+            if (lane >= o) x0 += y;
+        }
+        const int32_t total0 = __shfl_sync(kFull, x0, 31);
+        int32_t x1 = c1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(kFull, x1, o);
+            if (lane >= o) x1 += y;
+        }
+        int32_t b0 = x0 - c0, b1 = total0 + x1 - c1;  // block starts of labels lane, lane + 32
+        int32_t *o = off + v * (int64_t)(K + 1);
+        if (lane < K) o[lane] = b0;
+        if (lane + 32 < K) o[lane + 32] = b1;
+        if (lane == 0) o[K] = r.y - r.x;
+        for (int32_t base = r.x; base < r.y; base += 32) {
+            const int32_t i = base + lane;
+            const int32_t lab = i < r.y ? __ldg(g.label + i) : -1;
+            const int32_t nb = i < r.y ? __ldg(g.adj + i) : 0;
+            for (int32_t l = 0; l < K; ++l) {
+                const unsigned m = __ballot_sync(kFull, lab == l);
+                if (!m) continue;
+                const int32_t start = l < 32 ? __shfl_sync(kFull, b0, l) : __shfl_sync(kFull, b1, l - 32);
+                if (lab == l) nbr[r.x + start + __popc(m & ((1u << lane) - 1u))] = nb;
+                if (l == lane) b0 += __popc(m);
+                if (l == lane + 32) b1 += __popc(m);
+            }
+        }
+    }
+}
+
 constexpr int kEdgeRun = 8;  // consecutive CSR entries per thread in the edge-set kernels
 
 // Source vertex of CSR entry i: the largest v with rows[v].x <= i (rows of
@@ -367,6 +445,19 @@ cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, const 
 cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_max_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_label_range(const int32_t *label, int64_t e, int *lo_hi, cudaStream_t st) {
+    if (e <= 0) return cudaSuccess;
+    label_range_kernel<<<1024, 256, 0, st>>>(label, e, lo_hi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_label_index(const DevGraph &g, int32_t K, int32_t *off, int32_t *nbr, cudaStream_t st) {
+    if (g.n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>(((int64_t)g.n * 32 + 255) / 256, 152 * 64);
+    build_label_index_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, K, off, nbr);
     return cudaGetLastError();
 }
 

@@ -99,6 +99,14 @@ struct DevGraph {
     const unsigned long long *edges;
     int32_t edge_bits;
     int32_t edge_symmetric;
+    // MetaPath's label index (built by the first MetaPath ITS walk when every
+    // label lies in [0, lab_k), lab_k <= 64; null otherwise): lab_nbr holds
+    // each row's neighbours stably sorted by edge label (row order inside a
+    // label), lab_off[v * (lab_k + 1) + l] the row-relative start of label l's
+    // block and lab_off[v * (lab_k + 1) + lab_k] the degree.
+    const int32_t *lab_nbr;
+    const int32_t *lab_off;
+    int32_t lab_k;
     int32_t n;
     int64_t e;
 };
@@ -128,7 +136,10 @@ __device__ __forceinline__ bool edge_exists(const DevGraph &g, int32_t u, int32_
     return false;
 }
 
-enum Sampler : int { kUniform = 0, kITS = 1, kAlias = 2, kRejection = 3, kMaxRejection = 4 };
+// kLabelIndex: MetaPath's dynamic ITS answered from the label index (an
+// engine-internal sampler; it shares the ITS launch-shape slot)
+enum Sampler : int { kUniform = 0, kITS = 1, kAlias = 2, kRejection = 3, kMaxRejection = 4, kLabelIndex = 5 };
+constexpr int kMaxIndexedLabels = 64;
 enum Update : int { kFixedLength = 0, kGeometric = 1 };
 enum WeightKind : int { kEdgeWeight = 0, kUnitWeight = 1, kNode2Vec = 2, kLabelSchema = 3 };
 

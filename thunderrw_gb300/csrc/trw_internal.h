@@ -43,6 +43,11 @@ cudaError_t launch_collect_long_rows(const DevGraph &g, int2 *list, int *count, 
 // long_rows: the vertices of rows longer than 32 entries (longest first), one warp each
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, const int32_t *long_rows,
                                int32_t n_long, cudaStream_t st);
+// lo_hi[0] / lo_hi[1] (preset to INT_MAX / INT_MIN) become the smallest and
+// largest edge label
+cudaError_t launch_label_range(const int32_t *label, int64_t e, int *lo_hi, cudaStream_t st);
+// MetaPath's label index for labels in [0, K): off[n * (K + 1)], nbr[e]
+cudaError_t launch_build_label_index(const DevGraph &g, int32_t K, int32_t *off, int32_t *nbr, cudaStream_t st);
 // Node2Vec's edge set: `set` (2^bits slots) must hold kEdgeEmpty everywhere;
 // *symmetric must hold 1 and is cleared if some edge's reverse is missing.
 cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, int32_t bits, int *symmetric,

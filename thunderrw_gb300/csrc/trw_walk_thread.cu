@@ -237,6 +237,29 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
                 moved[r] = true;
             }
         }
+    } else if (S == kLabelIndex) {
+        // MetaPath's dynamic ITS over its 0/1 label weights (metapath.cpp:22-30,
+        // inverse_transformation_sampling.h:288-313): the upper bound over the
+        // 0/1 prefix sums picks match floor(count * real2) of the wanted label
+        // in row order, which the label index holds at lab_nbr[row + off[l] + m].
+        int32_t lo[R], cnt[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            cnt[r] = 0;
+            if (s[r].widx < 0) continue;
+            const int32_t want = p.schema[(s[r].len - 1) % p.schema_len];
+            if (s[r].crow.y <= s[r].crow.x || want < 0 || want >= g.lab_k) continue;  // no match: the walker stops
+            const int32_t *off = g.lab_off + (int64_t)s[r].cur * (g.lab_k + 1) + want;
+            lo[r] = __ldg(off);
+            cnt[r] = __ldg(off + 1) - lo[r];
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (cnt[r] <= 0) continue;
+            const int32_t m = (int32_t)((double)cnt[r] * real2(rnd[r].x));  // floor of P[last] * dr_
+            nxt[r] = __ldg(g.lab_nbr + s[r].crow.x + lo[r] + m);
+            moved[r] = true;
+        }
     } else if (S == kRejection) {
         // static_rs_move (rejection_sampling.h:334-366): trial k uses draws 2k, 2k+1.
         double mx[R];
@@ -436,7 +459,9 @@ cudaError_t launch_mode(const WalkParams &p, const LaunchShape &shape, cudaStrea
 // Sparse visit tables only exist for PPR (geometric update).
 template <int S, int U, int WK>
 cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
-    if (U == kGeometric && p.table) return launch_mode<S, U, WK, true>(p, shape, st);
+    if constexpr (U == kGeometric) {
+        if (p.table) return launch_mode<S, U, WK, true>(p, shape, st);
+    }
     return launch_mode<S, U, WK, false>(p, shape, st);
 }
 
@@ -454,6 +479,7 @@ cudaError_t launch_walk_thread(const WalkParams &p, int sampler, int update, int
                           : launch_shape<kITS, kFixedLength, kUnitWeight>(p, shape, st);
     case kRejection: return geo ? launch_shape<kRejection, kGeometric, kUnitWeight>(p, shape, st)
                                 : launch_shape<kRejection, kFixedLength, kUnitWeight>(p, shape, st);
+    case kLabelIndex: return launch_shape<kLabelIndex, kFixedLength, kLabelSchema>(p, shape, st);
     case kMaxRejection:
         if (weight_kind == kNode2Vec) return launch_shape<kMaxRejection, kFixedLength, kNode2Vec>(p, shape, st);
         if (weight_kind == kEdgeWeight) return launch_shape<kMaxRejection, kFixedLength, kEdgeWeight>(p, shape, st);

@@ -184,6 +184,13 @@ class Graph:
         N.check(_lib().trw_profile_read(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def indexes(self):
+        """(edge set, label index) states: 0 not built yet, 1 built, -1 not
+        applicable or no room (the walks then search, with the same results)."""
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        N.check(_lib().trw_graph_indexes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def device_error(self) -> int:
         c = ctypes.c_int32()
         N.check(_lib().trw_device_error(self._h, ctypes.byref(c)))
