@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="keep the automatic launch shape (no autotuning)")
+    ap.add_argument("--shape", default=None, help="walkers_per_lane,ctas_per_sm: set this launch shape, no tuning")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--dense", action="store_true", help="PPR: dense Q x N count output instead of sparse CSR")
     return ap.parse_args()
@@ -345,7 +346,12 @@ def run_ours(args):
     # ---- launch shape: tuned once on a sample of this workload, as a user
     # would (thunderrw_gb300/autotune.py), outside every timed region
     shape = None
-    if not args.no_tune:
+    if args.shape:
+        slot = "uniform" if args.workload == "ppr" else app.sampler
+        r, c = (int(x) for x in args.shape.split(","))
+        graph.set_engine_shape(slot, r, c)
+        shape = {"slot": slot, "walkers_per_lane": r, "ctas_per_sm": c, "set_by": "--shape"}
+    elif not args.no_tune:
         from thunderrw_gb300 import autotune
         if args.workload == "ppr":
             res = autotune.tune(graph, E.PPR(wl["tp"]), src, walkers_per_query=per_q, rings=(1, 2), ctas=(0, 4),
