@@ -41,6 +41,8 @@ def _slot(app: E.App, mode: Optional[str], sampler: Optional[str]) -> Tuple[str,
         return "uniform", False
     if app.name == "metapath" and m == "dynamic" and s == "its":
         return s, False  # the label index runs on the ring engine (the row scan ignores the ring)
+    if app.name in ("deepwalk", "genericwalk", "ppr"):
+        return s, False  # walker-independent weights: dynamic mode runs on the static tables
     return s, (m == "dynamic" and s in WARP_FAMILY)
 
 

@@ -111,6 +111,9 @@ struct trw_graph {
     int32_t *lab_off = nullptr;
     int32_t lab_k = 0;
     int lab_state = 0;
+    // every edge weight >= 0 and every non-empty row with a positive one:
+    // 0 = not checked yet, 1 = yes, -1 = no
+    int positive_rows = 0;
     int32_t edge_symmetric = 0;
     int edge_state = 0;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
@@ -282,6 +285,24 @@ int collect_long_rows(trw_graph *g, cudaStream_t st) {
     return TRW_OK;
 }
 
+// Whether the edge weights are all >= 0 with a positive one in every
+// non-empty row (checked once per graph).
+int check_positive_rows(trw_graph *g, cudaStream_t st, bool &ok) {
+    if (g->positive_rows == 0) {
+        int *d_bad = nullptr;
+        TRW_CUDA(cudaMalloc(&d_bad, sizeof(int)));
+        TRW_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), st));
+        TRW_CUDA(launch_positive_rows(dev_view(g), d_bad, st));
+        int bad = 0;
+        TRW_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TRW_CUDA(cudaStreamSynchronize(st));
+        cudaFree(d_bad);
+        g->positive_rows = bad ? -1 : 1;
+    }
+    ok = g->positive_rows == 1;
+    return TRW_OK;
+}
+
 int build_table(trw_graph *g, int sampler, int kind, cudaStream_t st) {
     const DevGraph d = dev_view(g);
     if (kind == TRW_WEIGHTS_EDGE && !g->weight) return fail(TRW_ERR_INVALID, "edge weights were not supplied");
@@ -440,6 +461,26 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     std::unique_lock<std::mutex> lock(g->mu, std::defer_lock);
     if (!hold_lock) lock.lock();
     TRW_CUDA(cudaSetDevice(g->device));
+    // Dynamic mode with walker-independent weights (DeepWalk and GenericWalk:
+    // edge weights; PPR: 1) gathers the same row every step, so its per-step
+    // ITS prefix, alias table or row maximum is the static one (same builder
+    // arithmetic in the same order, same draws): such walks run on the static
+    // tables.  Dynamic alias and rejection stop a walker on a row without a
+    // positive weight where the static forms move it, so they map only when
+    // the graph has no such row.
+    if (pl.warp_family && (pl.weight_kind == kEdgeWeight || pl.weight_kind == kUnitWeight) &&
+        (pl.sampler == kITS || pl.sampler == kAlias || pl.sampler == kRejection)) {
+        const int kind = pl.weight_kind == kUnitWeight ? TRW_WEIGHTS_UNIT : TRW_WEIGHTS_EDGE;
+        bool same = pl.sampler == kITS || kind == TRW_WEIGHTS_UNIT;
+        if (!same) {
+            rc = check_positive_rows(g, st, same);
+            if (rc) return rc;
+        }
+        if (same) {
+            pl.warp_family = false;
+            pl.table_kind = kind;
+        }
+    }
     if (pl.table_kind >= 0) {
         const int have = pl.sampler == kAlias ? g->alias_kind : pl.sampler == kITS ? g->prefix_kind : g->rmax_kind;
         if (have != pl.table_kind) {  // compute() rebuilds its static tables each run (creeper.h:700-702)

@@ -366,6 +366,24 @@ __global__ void build_label_index_kernel(const DevGraph g, int32_t K, int32_t *o
     }
 }
 
+// Sets *bad if an edge weight is negative or NaN, or a non-empty row has no
+// positive weight (one warp per row, grid-stride).
+__global__ void positive_rows_kernel(const DevGraph g, int *bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < g.n; v += warps) {
+        const int2 r = __ldg(g.rows + v);
+        bool neg = false, pos = false;
+        for (int32_t i = r.x + lane; i < r.y; i += 32) {
+            const double w = __ldg(g.weight + i);
+            neg |= !(w >= 0.0);
+            pos |= w > 0.0;
+        }
+        const bool any_neg = __any_sync(kFull, neg), any_pos = __any_sync(kFull, pos);
+        if (lane == 0 && (any_neg || (r.y > r.x && !any_pos))) atomicOr(bad, 1);
+    }
+}
+
 constexpr int kEdgeRun = 8;  // consecutive CSR entries per thread in the edge-set kernels
 
 // Source vertex of CSR entry i: the largest v with rows[v].x <= i (rows of
@@ -445,6 +463,13 @@ cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, const 
 cudaError_t launch_build_max(const DevGraph &g, int unit, double *out, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
     build_max_kernel<<<blocks_for(g.n), 256, 0, st>>>(g, unit, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_positive_rows(const DevGraph &g, int *bad, cudaStream_t st) {
+    if (g.n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>(((int64_t)g.n * 32 + 255) / 256, 152 * 64);
+    positive_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, bad);
     return cudaGetLastError();
 }
 

@@ -43,6 +43,8 @@ cudaError_t launch_collect_long_rows(const DevGraph &g, int2 *list, int *count, 
 // long_rows: the vertices of rows longer than 32 entries (longest first), one warp each
 cudaError_t launch_build_alias(const DevGraph &g, int unit, AliasSlot *out, const int32_t *long_rows,
                                int32_t n_long, cudaStream_t st);
+// *bad |= 1 if some edge weight is negative or NaN or a non-empty row has no positive weight
+cudaError_t launch_positive_rows(const DevGraph &g, int *bad, cudaStream_t st);
 // lo_hi[0] / lo_hi[1] (preset to INT_MAX / INT_MIN) become the smallest and
 // largest edge label
 cudaError_t launch_label_range(const int32_t *label, int64_t e, int *lo_hi, cudaStream_t st);

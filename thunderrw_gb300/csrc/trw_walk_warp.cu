@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_warp(const WalkParams p, in
                 __syncwarp();
             }
         }
-        if (S == kRejection && s.widx >= 0 && my_max > 0.0) {
+        if (S == kRejection && s.widx >= 0 && my_max != 0.0) {  // a zero row maximum stops the walker (creeper.h:283-293)
             // trials of dynamic_rs_move (rejection_sampling.h:404-436), per lane
             const int32_t deg = s.crow.y - s.crow.x;
             if (deg > 0) {

@@ -253,9 +253,11 @@ def compute(graph: Graph, sources, app: App, mode: Optional[str] = None, sampler
 
 def ppr_batch(graph: Graph, sources, walkers_per_query: int, tp: float = 0.2, seed: int = 1,
               counts: Optional[torch.Tensor] = None, zero_counts: bool = True, engine: str = "persistent",
-              stream=None):
+              stream=None, mode: str = "uniform", sampler: str = "uniform"):
     """Batched PPR: len(sources) queries x walkers_per_query walkers in one
-    launch; returns (counts[num_queries, n] int32 on the device, steps tensor)."""
+    launch; returns (counts[num_queries, n] int32 on the device, steps tensor).
+    `mode` / `sampler` as the reference's -em / -sm (PPR's hook weighs every
+    edge 1)."""
     dev = graph.device
     src = _dev(sources, torch.int32, dev)
     Q = src.numel()
@@ -263,7 +265,7 @@ def ppr_batch(graph: Graph, sources, walkers_per_query: int, tp: float = 0.2, se
         counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
         zero_counts = True
     steps = torch.zeros(1, dtype=torch.int64, device=dev)
-    d = PPR(tp).desc(seed)
+    d = PPR(tp, mode, sampler).desc(seed)
     N.check(_lib().trw_ppr_batch(graph.handle, ctypes.byref(d), _ptr(src), Q, int(walkers_per_query), _ptr(counts),
                                  _ptr(steps), 1 if zero_counts else 0, N.ENGINES[engine],
                                  ctypes.c_void_p(_stream_ptr(stream))))
