@@ -164,3 +164,31 @@ def test_sparse_order_with_wrapping_runs():
         assert torch.equal(a.counts[:total], b.counts[:total])
     finally:
         gr.close()
+
+
+@pytest.mark.parametrize("queries,wpq", [(1, 40_000), (3, 30_000)])
+def test_sparse_large_tables_split_over_ctas(queries, wpq):
+    """A query with many walkers gets a table of more than 2^16 slots, which
+    the post-processing splits over several CTAs: counts equal the oracle's
+    and the order is the same under both schedules."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("rmat", 1 << 17, 8, seed=23, weights=False)
+    row, adj = g["row"].numpy(), g["adj"].numpy()
+    qs = G.random_sources(g["row"], queries, seed=9).numpy()
+    og = O.Graph(row, adj)
+    ref = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=19), qs, per_query=wpq,
+                 want_counts=True, want_lengths=False)
+    gr = E.Graph(row, adj)
+    try:
+        a = E.ppr_batch_sparse(gr, qs, wpq, tp=0.2, seed=19, engine="persistent")
+        b = E.ppr_batch_sparse(gr, qs, wpq, tp=0.2, seed=19, engine="plain")
+        _check_against_dense(a, ref["counts"])
+        total = int(a.offsets[-1].item())
+        assert torch.equal(a.offsets, b.offsets)
+        assert torch.equal(a.vertices[:total], b.vertices[:total])
+        assert torch.equal(a.counts[:total], b.counts[:total])
+        again = E.ppr_batch_sparse(gr, qs, wpq, tp=0.2, seed=19)  # the tables were left clean
+        assert torch.equal(again.vertices[:total], a.vertices[:total])
+    finally:
+        gr.close()

@@ -791,7 +791,8 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         g->ppr_bits = bits;
         g->ppr_queries = num_queries;
     }
-    const size_t b_dist = align_up(sizeof(int32_t) * 17 * (size_t)std::max<int64_t>(1, num_queries));
+    const int64_t dist_ints = ppr_distinct_ints(bits);  // per query: total + segment prefixes
+    const size_t b_dist = align_up(sizeof(int32_t) * (size_t)dist_ints * (size_t)std::max<int64_t>(1, num_queries));
     TRW_CUDA(g->ppr_distinct.ensure(b_dist + sizeof(uint64_t) * (kMaxRanges + 1)));
     int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
     int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
@@ -863,7 +864,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         const int64_t nq = std::min(per, num_queries - qs);
         const cudaStream_t sr = rs[nr & 1];
         int32_t *tab = tables + (qs << (bits + 1));
-        int32_t *dist = distinct + 17 * qs;
+        int32_t *dist = distinct + dist_ints * qs;
         int rc = run_walk(g, desc, d_src + qs, nq, nq * walkers_per_query, walkers_per_query, qs * walkers_per_query,
                           nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, sr, tab, bits,
                           /*hold_lock=*/true);

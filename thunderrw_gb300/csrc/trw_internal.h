@@ -31,7 +31,9 @@ int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
 // offsets[0] must hold the entries before this range of queries (0 for the first)
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st);
-// `distinct` holds nq totals followed by nq x 16 segment counts
+// `distinct` holds nq totals followed by ppr_distinct_ints(bits) - 1 segment
+// prefixes per query (ppr_distinct_ints(bits) ints per query in all)
+int64_t ppr_distinct_ints(int32_t bits);
 cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
                             const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
                             cudaStream_t st);

@@ -8,11 +8,13 @@
 // whole count array zeroed every batch.
 //
 // After the walk:
-//  * distinct_kernel + offsets_kernel: occupied slots per query, then their
-//    exclusive scan into CSR offsets (offsets[q] .. offsets[q+1] hold query
+//  * distinct_kernel + segment_scan_kernel + offsets_kernel: occupied slots
+//    per warp segment of each table, their prefix within the query, then the
+//    queries' totals scanned into CSR offsets (offsets[q] .. offsets[q+1] hold query
 //    q's entries), continuing from offsets[0] so that a batch can run as
 //    several ranges of queries;
-//  * emit_kernel (one CTA per query): writes the (vertex, count) pairs.  With
+//  * emit_kernel (one CTA per chunk of at most 2^16 slots): writes the
+//    (vertex, count) pairs.  With
 //    linear probing the SET of occupied slots does not depend on the order of
 //    insertion, only the order of keys inside each run of occupied slots
 //    does; so the kernel emits runs in slot order (the run that wraps around
@@ -56,32 +58,54 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T &total) {
     return excl;
 }
 
-constexpr int kEmitWarps = kEmitThreads / 32;  // table segments per query
+constexpr int kEmitWarps = kEmitThreads / 32;  // table segments per CTA
+constexpr int32_t kChunkBits = 16;             // at most 2^16 slots per CTA
 
-// Occupied slots (distinct visited vertices) of each query's table, per
-// segment of 1/kEmitWarps of the slots (the emit kernel's warp split) and in
-// total.
-__global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *tables, int32_t bits, int32_t *distinct,
-                                                                int32_t *seg_counts) {
-    const int64_t q = blockIdx.x;
+// A table of 2^bits slots is split into chunks_for(bits) chunks of at most
+// 2^16 slots, one CTA each, and every chunk into kEmitWarps warp segments;
+// a single large table (a query with many walkers) is then spread over the
+// GPU instead of one CTA.
+__host__ __device__ inline uint32_t chunks_for(int32_t bits) {
+    return bits > kChunkBits ? 1u << (bits - kChunkBits) : 1u;
+}
+
+// Occupied slots (distinct visited vertices) per warp segment: seg[(q * S +
+// chunk) * kEmitWarps + warp].
+__global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *tables, int32_t bits, int32_t *seg) {
+    const uint32_t S = chunks_for(bits);
+    const int64_t q = blockIdx.x / S;
+    const uint32_t c = blockIdx.x % S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t seg4 = (1u << bits) / kEmitWarps / 4;  // int4 per segment
-    const int4 *keys = reinterpret_cast<const int4 *>(tables + (q << (bits + 1))) + warp * seg4;
-    uint32_t c = 0;
+    const uint32_t chunk = (1u << bits) / S;
+    const uint32_t seg4 = chunk / kEmitWarps / 4;  // int4 per segment
+    const int4 *keys = reinterpret_cast<const int4 *>(tables + (q << (bits + 1)) + (size_t)c * chunk) + warp * seg4;
+    uint32_t n = 0;
     for (uint32_t i = lane; i < seg4; i += 32) {
         const int4 k = __ldg(keys + i);
-        c += (k.x != 0) + (k.y != 0) + (k.z != 0) + (k.w != 0);
+        n += (k.x != 0) + (k.y != 0) + (k.z != 0) + (k.w != 0);
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    __shared__ uint32_t ws[kEmitWarps];
-    if (lane == 0) { ws[warp] = c; seg_counts[q * kEmitWarps + warp] = (int32_t)c; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < kEmitWarps; ++w) t += ws[w];
-        distinct[q] = (int32_t)t;
+    for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (lane == 0) seg[((int64_t)blockIdx.x) * kEmitWarps + warp] = (int32_t)n;
+}
+
+// Per query: the segment counts become their exclusive prefix within the
+// query (in place) and the query's total goes to distinct[q].
+__global__ void __launch_bounds__(kScanThreads) segment_scan_kernel(int32_t *seg, int32_t bits, int32_t *distinct) {
+    __shared__ int32_t sums[32];
+    const int64_t q = blockIdx.x;
+    const int32_t n = (int32_t)chunks_for(bits) * kEmitWarps;
+    int32_t *v = seg + q * n;
+    int32_t carry = 0;
+    for (int32_t b = 0; b < n; b += kScanThreads) {
+        const int32_t i = b + threadIdx.x;
+        const int32_t x = i < n ? v[i] : 0;
+        int32_t total;
+        const int32_t ex = block_exclusive_scan<int32_t>(x, sums, total);
+        if (i < n) v[i] = carry + ex;
+        carry += total;
     }
+    if (threadIdx.x == 0) distinct[q] = carry;
 }
 
 // offsets[0] holds the entries of the queries before this range (0 for the
@@ -100,7 +124,8 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
     if (threadIdx.x == 0) offsets[nq] = carry;
 }
 
-// One CTA per query, one contiguous segment of the table per warp.
+// One CTA per chunk of at most 2^16 slots of a query's table, one contiguous
+// segment of the chunk per warp.
 //
 // Output order.  Inserts probe linearly and wrap from the last slot to slot
 // 0, so the occupied slots form maximal runs on a cycle; which slots are
@@ -119,10 +144,12 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 // 96-slot window, and the wrapping run, are read from global memory, which
 // stays intact until the final zeroing.
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, const int64_t *offsets,
-                                                            const int32_t *seg_counts, int32_t *vout, int32_t *cout,
+                                                            const int32_t *seg_prefix, int32_t *vout, int32_t *cout,
                                                             int64_t capacity, int *error) {
     __shared__ uint32_t wrap[2];
-    const int64_t q = blockIdx.x;
+    const uint32_t S = chunks_for(bits);
+    const int64_t q = blockIdx.x / S;
+    const uint32_t chunk = blockIdx.x % S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nslots = 1u << bits;
     int32_t *keys = tables + (q << (bits + 1));
@@ -130,7 +157,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     const int64_t end = offsets[q + 1];
     const bool write = end <= capacity;
     if (threadIdx.x == 0) {
-        if (!write) atomicOr(error, kErrCapacity);
+        if (!write && chunk == 0) atomicOr(error, kErrCapacity);
         // the wrapping run: `head` slots from slot 0 and `tail` slots before the end
         uint32_t head = 0, tail = 0;
         if (__ldg(keys) != 0 && __ldg(keys + nslots - 1) != 0) {
@@ -146,11 +173,10 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     }
     __syncthreads();
     const uint32_t head = wrap[0], tail = wrap[1], cyc = head + tail;
-    int64_t prefix = offsets[q];
-    for (int w = 0; w < warp; ++w) prefix += seg_counts[q * kEmitWarps + w];
+    int64_t prefix = offsets[q] + seg_prefix[(int64_t)blockIdx.x * kEmitWarps + warp];
 
-    const uint32_t seg = nslots / kEmitWarps;  // >= 64: tables have >= 1024 slots
-    const uint32_t lo = warp * seg, nblk = seg / 32;
+    const uint32_t seg = nslots / S / kEmitWarps;  // >= 64: tables have >= 1024 slots, chunks 2^16
+    const uint32_t lo = chunk * (nslots / S) + warp * seg, nblk = seg / 32;
     const uint32_t x0 = lo + lane;
     auto key_at = [&](uint32_t y) { return y < nslots ? __ldg(keys + y) : 0; };
     auto cnt_at = [&](uint32_t y) { return y < nslots ? __ldg(cnts + y) : 0; };
@@ -229,11 +255,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
         kn = k2; cn = c2;
         k2 = k3; c2 = c3;
     }
-    if (threadIdx.x == 0) {
-        int64_t t = 0;
-        for (int w = 0; w < kEmitWarps; ++w) t += seg_counts[q * kEmitWarps + w];
-        if (t != offsets[q + 1] - offsets[q]) atomicOr(error, kErrCapacity);
-    }
+    if (S > 1) return;  // chunked tables are zeroed after the kernel: other CTAs may still read this chunk
     __syncthreads();
     // zero the table for the next batch (coalesced 16-byte stores)
     int4 *z = reinterpret_cast<int4 *>(keys);
@@ -254,9 +276,15 @@ cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaSt
     return cudaGetLastError();
 }
 
+int64_t ppr_distinct_ints(int32_t bits) { return 1 + (int64_t)chunks_for(bits) * kEmitWarps; }
+
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st) {
-    if (nq > 0) distinct_kernel<<<(unsigned)nq, kEmitThreads, 0, st>>>(tables, bits, distinct, distinct + nq);
+    if (nq > 0) {
+        const int64_t ctas = nq * chunks_for(bits);
+        distinct_kernel<<<(unsigned)ctas, kEmitThreads, 0, st>>>(tables, bits, distinct + nq);
+        segment_scan_kernel<<<(unsigned)nq, kScanThreads, 0, st>>>(distinct + nq, bits, distinct);
+    }
     offsets_kernel<<<1, kScanThreads, 0, st>>>(distinct, nq, offsets);
     return cudaGetLastError();
 }
@@ -265,8 +293,10 @@ cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int
                             const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
                             cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
-    emit_kernel<<<(unsigned)nq, kEmitThreads, 0, st>>>(tables, bits, offsets, distinct + nq, vout, cout, capacity,
-                                                       error);
+    const uint32_t S = chunks_for(bits);
+    emit_kernel<<<(unsigned)(nq * S), kEmitThreads, 0, st>>>(tables, bits, offsets, distinct + nq, vout, cout,
+                                                             capacity, error);
+    if (S > 1) return cudaMemsetAsync(tables, 0, sizeof(int32_t) * 2 * ((size_t)nq << bits), st);
     return cudaGetLastError();
 }
 
