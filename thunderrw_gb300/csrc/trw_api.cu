@@ -445,6 +445,22 @@ void fill_app_params(WalkParams &p, const trw_walk_desc *desc) {
     p.seed = desc->seed;
 }
 
+// Streams, events and pinned words of the host-output pipelines (created on
+// first use).
+int ensure_host_pipeline(trw_graph *g) {
+    if (!g->copy_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (!g->aux_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
+    if (!g->h_ends) TRW_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&g->h_ends), sizeof(int64_t) * kMaxRanges,
+                                           cudaHostAllocDefault));
+    for (cudaEvent_t *e : {&g->ev_fork, &g->ev_join})
+        if (!*e) TRW_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (int r = 0; r < kMaxRanges; ++r) {
+        if (!g->range_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->range_done[r], cudaEventDisableTiming));
+        if (!g->offsets_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->offsets_done[r], cudaEventDisableTiming));
+    }
+    return TRW_OK;
+}
+
 // Shared implementation of trw_walk and trw_ppr_batch.
 int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
              int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
@@ -622,6 +638,88 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     return TRW_OK;
 }
 
+// trw_walk into host paths / lengths for a large batch: the walkers run as
+// ranges alternating between two compute streams, and each range's paths
+// and lengths are copied to the host on the copy stream while the next range
+// walks (the pipeline of the sparse PPR batches).  Walker ids continue across
+// ranges, so the walks are exactly those of one launch.  `taken` stays false
+// (and nothing runs) when the batch is too small for two ranges of at least
+// two walkers per lane, or when the outputs are on the device.
+int walk_host_ranges(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t W, int64_t id_base,
+                     int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts, uint64_t *steps,
+                     int32_t engine, cudaStream_t st, bool &taken) {
+    taken = false;
+    if (!g || !desc || W <= 0 || !sources || (paths && path_cap <= 0)) return TRW_OK;
+    const bool h_paths = paths && !is_device_ptr(paths);
+    const bool h_len = lengths && !is_device_ptr(lengths);
+    if ((!h_paths && !h_len) || (paths && !h_paths) || (lengths && !h_len)) return TRW_OK;
+    const int64_t lanes = (int64_t)g->num_sms * 2048;
+    const int64_t ranges = std::min<int64_t>(kMaxRanges, W / (2 * lanes));
+    if (ranges < 2) return TRW_OK;
+    taken = true;
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    int rc = ensure_host_pipeline(g);
+    if (rc) return rc;
+    const bool h_src = !is_device_ptr(sources);
+    const bool h_cnt = counts && !is_device_ptr(counts);
+    const bool h_steps = steps && !is_device_ptr(steps);
+    const size_t b_src = h_src ? align_up(sizeof(int32_t) * (size_t)W) : 0;
+    const size_t b_cnt = h_cnt ? align_up(sizeof(int32_t) * (size_t)g->n) : 0;
+    TRW_CUDA(g->stage.ensure(b_src + b_cnt + sizeof(uint64_t) * (kMaxRanges + 1)));
+    char *sb = static_cast<char *>(g->stage.p);
+    const int32_t *d_src = h_src ? reinterpret_cast<const int32_t *>(sb) : sources;
+    int32_t *d_cnt = h_cnt ? reinterpret_cast<int32_t *>(sb + b_src) : counts;
+    uint64_t *d_steps = reinterpret_cast<uint64_t *>(sb + b_src + b_cnt);
+    const size_t b_paths = paths ? align_up(sizeof(int32_t) * (size_t)W * (size_t)path_cap) : 0;
+    TRW_CUDA(g->stage_out.ensure(b_paths + (lengths ? align_up(sizeof(int32_t) * (size_t)W) : 0) + 256));
+    int32_t *d_paths = paths ? static_cast<int32_t *>(g->stage_out.p) : nullptr;
+    int32_t *d_len = lengths ? reinterpret_cast<int32_t *>(static_cast<char *>(g->stage_out.p) + b_paths) : nullptr;
+    if (h_src) TRW_CUDA(cudaMemcpyAsync((void *)d_src, sources, sizeof(int32_t) * (size_t)W, cudaMemcpyHostToDevice, st));
+    // trw_walk adds to the caller's counts
+    if (h_cnt) TRW_CUDA(cudaMemcpyAsync(d_cnt, counts, sizeof(int32_t) * (size_t)g->n, cudaMemcpyHostToDevice, st));
+    TRW_CUDA(cudaEventRecord(g->ev_fork, st));
+    TRW_CUDA(cudaStreamWaitEvent(g->aux_stream, g->ev_fork, 0));
+    const cudaStream_t rs[2] = {st, g->aux_stream};
+    const int64_t per = (W + ranges - 1) / ranges;
+    int nr = 0;
+    for (int64_t ws = 0; ws < W; ws += per, ++nr) {
+        const int64_t n = std::min(per, W - ws);
+        rc = run_walk(g, desc, d_src + ws, n, n, 0, id_base + ws, d_paths ? d_paths + ws * path_cap : nullptr,
+                      path_cap, d_len ? d_len + ws : nullptr, d_cnt, counts ? (int64_t)g->n : 0, false, d_steps + nr,
+                      engine, rs[nr & 1], nullptr, 0, /*hold_lock=*/true);
+        if (rc) return rc;
+        TRW_CUDA(cudaEventRecord(g->range_done[nr], rs[nr & 1]));
+    }
+    TRW_CUDA(cudaEventRecord(g->ev_join, g->aux_stream));
+    TRW_CUDA(cudaStreamWaitEvent(st, g->ev_join, 0));
+    if (steps) {
+        uint64_t *sum = h_steps ? d_steps + kMaxRanges : steps;
+        TRW_CUDA(launch_sum_steps(d_steps, nr, sum, st));
+        if (h_steps) TRW_CUDA(cudaMemcpyAsync(steps, sum, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    }
+    if (h_cnt) TRW_CUDA(cudaMemcpyAsync(counts, d_cnt, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, st));
+    int64_t ws = 0;
+    for (int r = 0; r < nr; ++r, ws += per) {
+        const int64_t n = std::min(per, W - ws);
+        TRW_CUDA(cudaEventSynchronize(g->range_done[r]));
+        if (paths) TRW_CUDA(cudaMemcpyAsync(paths + ws * path_cap, d_paths + ws * path_cap,
+                                            sizeof(int32_t) * (size_t)n * (size_t)path_cap, cudaMemcpyDeviceToHost,
+                                            g->copy_stream));
+        if (lengths) TRW_CUDA(cudaMemcpyAsync(lengths + ws, d_len + ws, sizeof(int32_t) * (size_t)n,
+                                              cudaMemcpyDeviceToHost, g->copy_stream));
+    }
+    TRW_CUDA(cudaStreamSynchronize(st));
+    TRW_CUDA(cudaStreamSynchronize(g->copy_stream));
+    int err = 0;
+    TRW_CUDA(cudaMemcpy(&err, g->error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        TRW_CUDA(cudaMemset(g->error, 0, sizeof(int)));
+        return fail(TRW_ERR_DEVICE, "device error word %d (1 = rejection trial limit, 2 = invalid source vertex)", err);
+    }
+    return TRW_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -747,6 +845,10 @@ int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t o
 int trw_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_walkers, int64_t id_base,
              int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts, uint64_t *steps, int32_t engine,
              trw_stream_t stream) {
+    bool taken = false;
+    const int rc = walk_host_ranges(g, desc, sources, num_walkers, id_base, paths, path_cap, lengths, counts, steps,
+                                    engine, reinterpret_cast<cudaStream_t>(stream), taken);
+    if (taken) return rc;
     return run_walk(g, desc, sources, num_walkers, num_walkers, 0, id_base, paths, path_cap, lengths, counts,
                     g ? (int64_t)g->n : 0, false, steps, engine, reinterpret_cast<cudaStream_t>(stream));
 }
@@ -837,16 +939,8 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kMaxRanges, num_queries), by_walkers));
     }
     if (host_out) {
-        if (!g->copy_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
-        if (!g->aux_stream) TRW_CUDA(cudaStreamCreateWithFlags(&g->aux_stream, cudaStreamNonBlocking));
-        if (!g->h_ends) TRW_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&g->h_ends), sizeof(int64_t) * kMaxRanges,
-                                               cudaHostAllocDefault));
-        for (cudaEvent_t *e : {&g->ev_fork, &g->ev_join})
-            if (!*e) TRW_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-        for (int r = 0; r < kMaxRanges; ++r) {
-            if (!g->range_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->range_done[r], cudaEventDisableTiming));
-            if (!g->offsets_done[r]) TRW_CUDA(cudaEventCreateWithFlags(&g->offsets_done[r], cudaEventDisableTiming));
-        }
+        const int rc = ensure_host_pipeline(g);
+        if (rc) return rc;
     }
 
     // Walker ids continue across ranges (id_base = first query x walkers per
