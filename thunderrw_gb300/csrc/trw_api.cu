@@ -688,7 +688,12 @@ int walk_host_ranges(trw_graph *g, const trw_walk_desc *desc, const int32_t *sou
         rc = run_walk(g, desc, d_src + ws, n, n, 0, id_base + ws, d_paths ? d_paths + ws * path_cap : nullptr,
                       path_cap, d_len ? d_len + ws : nullptr, d_cnt, counts ? (int64_t)g->n : 0, false, d_steps + nr,
                       engine, rs[nr & 1], nullptr, 0, /*hold_lock=*/true);
-        if (rc) return rc;
+        if (rc) {
+            // ranges already queued still write the staging buffers: let them finish before returning
+            cudaStreamSynchronize(g->aux_stream);
+            cudaStreamSynchronize(st);
+            return rc;
+        }
         TRW_CUDA(cudaEventRecord(g->range_done[nr], rs[nr & 1]));
     }
     TRW_CUDA(cudaEventRecord(g->ev_join, g->aux_stream));
@@ -962,7 +967,12 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         int rc = run_walk(g, desc, d_src + qs, nq, nq * walkers_per_query, walkers_per_query, qs * walkers_per_query,
                           nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, sr, tab, bits,
                           /*hold_lock=*/true);
-        if (rc) return rc;
+        if (rc) {
+            // earlier ranges are still queued on both streams: let them finish before returning
+            if (rs[1] != st) cudaStreamSynchronize(rs[1]);
+            cudaStreamSynchronize(st);
+            return rc;
+        }
         if (nr > 0 && rs[1] != st) TRW_CUDA(cudaStreamWaitEvent(sr, g->offsets_done[nr - 1], 0));
         TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, sr));
         if (host_out) TRW_CUDA(cudaEventRecord(g->offsets_done[nr], sr));
