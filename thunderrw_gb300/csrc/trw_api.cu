@@ -69,7 +69,12 @@ struct EngineSlot {
 };
 
 constexpr int kEngineSlots = 64;
-constexpr int kMaxRanges = 16;  // query ranges of a sparse PPR batch with host outputs
+constexpr int kMaxRanges = 16;  // walker ranges of a host-output walk (the pipelines' event arrays)
+// Query ranges of a sparse PPR batch with host outputs: the 4096 x 10^4
+// batch on R-MAT 2^22 takes 9.8 / 9.06 / 9.24 ms end to end at 4 / 8 / 16
+// ranges (each range boundary costs a walk tail; too few leave the last
+// range's copy exposed).
+constexpr int kPprRanges = 8;
 
 int app_weight_kind(int app) {
     switch (app) {
@@ -929,7 +934,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
                                  cudaMemcpyHostToDevice, st));
     }
 
-    // With host outputs the batch runs as up to kMaxRanges ranges of queries:
+    // With host outputs the batch runs as up to kPprRanges ranges of queries:
     // while one range walks, the copy stream moves the previous range's
     // entries to the host (a device-to-host copy runs at about half the rate
     // the entries are produced, so it hides behind the next walk).  Ranges
@@ -941,7 +946,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     if (host_out && num_queries > 1) {
         const int64_t lanes = (int64_t)g->num_sms * 2048;
         const int64_t by_walkers = num_queries * walkers_per_query / (8 * lanes);
-        ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kMaxRanges, num_queries), by_walkers));
+        ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kPprRanges, num_queries), by_walkers));
     }
     if (host_out) {
         const int rc = ensure_host_pipeline(g);
