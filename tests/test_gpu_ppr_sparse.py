@@ -192,3 +192,44 @@ def test_sparse_large_tables_split_over_ctas(queries, wpq):
         assert torch.equal(again.vertices[:total], a.vertices[:total])
     finally:
         gr.close()
+
+
+def test_sparse_host_weighted_ranges(rmat):
+    """A batch of at least 16 units of 8 walkers per lane (and 32 queries)
+    runs as 10 query ranges weighted 1,1,2,2,2,2,2,2,1,1 (half-size first and
+    last ranges); the result equals the one-range device-output batch and the
+    oracle for queries of a small first range, a middle range and the small
+    last range."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+    Q, wpq = 40, 1_000_000  # 40 M walkers >= 16 x 8 walkers per lane of 152 SMs
+    qs = G.random_sources(torch.from_numpy(rmat["row"]), Q, seed=12)
+    g = E.Graph(rmat["row"], rmat["adj"])
+    try:
+        dev = E.ppr_batch_sparse(g, qs, wpq, tp=0.2, seed=51)
+        need = int(dev.offsets[-1].item())
+        L = N.load()
+        off = torch.zeros(Q + 1, dtype=torch.int64).pin_memory()
+        v = torch.zeros(need, dtype=torch.int32).pin_memory()
+        c = torch.zeros(need, dtype=torch.int32).pin_memory()
+        steps = torch.zeros(1, dtype=torch.int64).pin_memory()
+        src = qs.to(torch.int32).contiguous().pin_memory()
+        d = E.PPR(0.2).desc(51)
+        rc = L.trw_ppr_batch_sparse(g.handle, ctypes.byref(d), src.data_ptr(), Q, wpq, off.data_ptr(), v.data_ptr(),
+                                    c.data_ptr(), need, steps.data_ptr(), 0, None)
+        assert rc == 0, L.trw_last_error()
+        assert int(steps[0]) == dev.steps
+        assert torch.equal(off, dev.offsets.cpu())
+        assert torch.equal(v, dev.vertices[:need].cpu())
+        assert torch.equal(c, dev.counts[:need].cpu())
+        og = O.Graph(rmat["row"], rmat["adj"])
+        for q in (1, 20, 39):  # ranges [0, 2), [20, 25) and [37, 40) of 40 queries
+            ref = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=51),
+                         qs.numpy()[q:q + 1], per_query=wpq, id_base=q * wpq, want_counts=True, want_lengths=False)
+            lo, hi = int(off[q]), int(off[q + 1])
+            dense = np.zeros(g.n, dtype=np.int32)
+            dense[v[lo:hi].numpy()] = c[lo:hi].numpy()
+            np.testing.assert_array_equal(dense, ref["counts"][0])
+    finally:
+        g.close()

@@ -70,11 +70,17 @@ struct EngineSlot {
 
 constexpr int kEngineSlots = 64;
 constexpr int kMaxRanges = 16;  // walker ranges of a host-output walk (the pipelines' event arrays)
-// Query ranges of a sparse PPR batch with host outputs: the 4096 x 10^4
-// batch on R-MAT 2^22 takes 9.8 / 9.06 / 9.24 ms end to end at 4 / 8 / 16
-// ranges (each range boundary costs a walk tail; too few leave the last
-// range's copy exposed).
+// Query ranges of a sparse PPR batch with host outputs.  The 4096 x 10^4
+// batch on R-MAT 2^22 takes 9.8 / 9.17 / 9.24 ms end to end at 4 / 8 / 16
+// equal ranges (each range boundary costs a walk tail; too few leave the
+// last range's copy exposed) and 8.80 ms as 10 ranges weighted
+// 1,1,2,2,2,2,2,2,1,1: the small first ranges start the copies early and
+// the small last ones leave little copy after the final walk.  Batches with
+// fewer than 16 units of 8 walkers per lane use at most kPprRanges equal
+// ranges.
 constexpr int kPprRanges = 8;
+constexpr int kPprSplit[] = {1, 1, 2, 2, 2, 2, 2, 2, 1, 1};
+constexpr int kPprSplitUnits = 16;  // sum of kPprSplit
 
 int app_weight_kind(int app) {
     switch (app) {
@@ -934,20 +940,36 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
                                  cudaMemcpyHostToDevice, st));
     }
 
-    // With host outputs the batch runs as up to kPprRanges ranges of queries:
-    // while one range walks, the copy stream moves the previous range's
-    // entries to the host (a device-to-host copy runs at about half the rate
-    // the entries are produced, so it hides behind the next walk).  Ranges
+    // With host outputs the batch runs as several ranges of queries (split
+    // by kPprSplit, or up to kPprRanges equal ones): while one range walks,
+    // the copy stream moves the previous range's entries to the host (a
+    // device-to-host copy runs at about half the rate the entries are
+    // produced, so it hides behind the next walk).  Ranges
     // alternate between two compute streams so that the next range's walk
     // fills the GPU while the last walkers of a range finish; only the
     // offsets scans are chained across ranges.  Every range keeps at least 8
-    // walkers per lane of the GPU.
-    int ranges = 1;
+    // walkers per lane of the GPU.  bounds[r] .. bounds[r + 1] = range r.
+    std::vector<int64_t> bounds{0};
     if (host_out && num_queries > 1) {
         const int64_t lanes = (int64_t)g->num_sms * 2048;
         const int64_t by_walkers = num_queries * walkers_per_query / (8 * lanes);
-        ranges = (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kPprRanges, num_queries), by_walkers));
+        if (by_walkers >= kPprSplitUnits && num_queries >= 2 * kPprSplitUnits) {
+            int64_t acc = 0;
+            for (int w : kPprSplit) {
+                acc += w;
+                bounds.push_back(num_queries * acc / kPprSplitUnits);
+            }
+        } else {
+            const int64_t n = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(kPprRanges, num_queries),
+                                                                     by_walkers));
+            const int64_t per = (num_queries + n - 1) / n;
+            for (int64_t qs = per; qs < num_queries; qs += per) bounds.push_back(qs);
+            bounds.push_back(num_queries);
+        }
+    } else if (num_queries > 0) {
+        bounds.push_back(num_queries);
     }
+    const int ranges = (int)bounds.size() - 1;  // 0 for an empty batch
     if (host_out) {
         const int rc = ensure_host_pipeline(g);
         if (rc) return rc;
@@ -956,7 +978,6 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     // Walker ids continue across ranges (id_base = first query x walkers per
     // query), so the walks do not depend on how the batch is split.
     TRW_CUDA(cudaMemsetAsync(d_off, 0, sizeof(int64_t), st));
-    const int64_t per = num_queries > 0 ? (num_queries + ranges - 1) / ranges : 0;
     const cudaStream_t rs[2] = {st, ranges > 1 ? g->aux_stream : st};
     if (rs[1] != st) {
         TRW_CUDA(cudaEventRecord(g->ev_fork, st));
@@ -964,8 +985,8 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     }
     int nr = 0;
     g->ppr_dirty = true;
-    for (int64_t qs = 0; qs < num_queries; qs += per, ++nr) {
-        const int64_t nq = std::min(per, num_queries - qs);
+    for (; nr < ranges; ++nr) {
+        const int64_t qs = bounds[nr], nq = bounds[nr + 1] - qs;
         const cudaStream_t sr = rs[nr & 1];
         int32_t *tab = tables + (qs << (bits + 1));
         int32_t *dist = distinct + dist_ints * qs;
