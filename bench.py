@@ -573,7 +573,7 @@ def run_ours(args):
 
 def run_serving(args):
     """Serving mix: Poisson arrivals at swept rates on a resident R-MAT graph
-    (alias + ITS tables built), apps uniform over PPR / DeepWalk / Node2Vec /
+    (alias + ITS tables, edge set and label index built), apps uniform over PPR / DeepWalk / Node2Vec /
     MetaPath, walkers log-uniform in [1e3, 1e6], lengths uniform in [5, 80].
     Reports p50 / p99 latency (submit -> results complete in HBM) and steps/s
     per arrival rate."""
@@ -593,6 +593,7 @@ def run_serving(args):
     t0 = time.perf_counter()
     graph.build_tables("alias", "edge")
     graph.build_tables("its", "edge")
+    indexes = graph.build_indexes()  # Node2Vec edge set, MetaPath label index: no request builds them
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     rng = np.random.default_rng(5)
@@ -640,8 +641,9 @@ def run_serving(args):
     line = {"metric": "walk_steps_per_s", "value": best["steps_per_s"], "unit": "steps/s", "n_gpus": 1,
             "steps": len(results), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+f64", "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": "serving mix rmat N=2^%d deg=32, 5 labels, alias+ITS resident" % scale,
-                       "n": graph.n, "e": graph.e, "table_build_s": build_s},
+            "config": {"workload": "serving mix rmat N=2^%d deg=32, 5 labels, alias+ITS tables, edge set and label index resident" % scale,
+                       "n": graph.n, "e": graph.e, "table_build_s": build_s,
+                       "indexes": {"edge_set": indexes[0], "label_index": indexes[1]}},
             "serving": results}
     print(json.dumps(line), flush=True)
     graph.close()

@@ -137,6 +137,14 @@ int trw_graph_synchronize(trw_graph *g);
  * same either way. */
 int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *label_index_state);
 
+/* Builds those lookup structures now instead of in the first walk that needs
+ * them, e.g. before a serving loop starts so that no request pays for a
+ * build (the reference builds everything it needs before compute() starts
+ * its timer, creeper.h:700-766).  Nonzero flags select the structures; one
+ * already built, not applicable or without room is left as it is (read the
+ * states with trw_graph_indexes).  Synchronises the stream. */
+int trw_graph_build_indexes(trw_graph *g, int32_t edge_set, int32_t label_index, trw_stream_t stream);
+
 /* ---- static tables ---------------------------------------------------- */
 
 /* Replaces static_initialization (creeper.h:102-175) and the offline

@@ -50,3 +50,32 @@ def test_metapath_index_matches_oracle(labels, schema, want_state):
             assert (r.lengths.cpu().numpy() == 4).any()
     finally:
         g.close()
+
+
+def test_build_indexes_up_front():
+    """trw_graph_build_indexes builds the Node2Vec edge set and the MetaPath
+    label index before any walk; walks then equal the oracle's (searching)
+    walks, and a second build call changes nothing."""
+    torch, E = need_gpu()
+    row, adj, lab = _graph()
+    w = np.ones(adj.size)
+    src = np.nonzero(np.diff(row))[0].astype(np.int32)
+    og = O.Graph(row, adj, w, lab)
+    g = E.Graph(row, adj, w, lab)
+    try:
+        assert g.indexes() == (0, 0)
+        assert g.build_indexes(edge_set=False, label_index=True) == (0, 1)
+        assert g.build_indexes() == (1, 1)
+        assert g.build_indexes() == (1, 1)
+        cases = [(E.MetaPath(12, [0, 1, 2, 3, 4]), O.make_desc("metapath", "dynamic", "its", length=12,
+                                                              schema=[0, 1, 2, 3, 4], seed=23)),
+                 (E.Node2Vec(12, 2.0, 0.5), O.make_desc("node2vec", "dynamic", "maxweight_rejection", length=12,
+                                                       p=2.0, q=0.5, seed=23))]
+        for app, d in cases:
+            ref = O.walk(og, d, src, path_cap=12)
+            r = E.compute(g, src, app, seed=23)
+            np.testing.assert_array_equal(r.paths.cpu().numpy(), ref["paths"])
+            assert r.steps == ref["steps"]
+        assert g.indexes() == (1, 1)
+    finally:
+        g.close()

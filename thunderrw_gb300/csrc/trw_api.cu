@@ -830,6 +830,23 @@ int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *labe
     return TRW_OK;
 }
 
+int trw_graph_build_indexes(trw_graph *g, int32_t edge_set, int32_t label_index, trw_stream_t stream) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (edge_set) {
+        const int rc = build_edge_set(g, st);
+        if (rc) return rc;
+    }
+    if (label_index) {
+        const int rc = build_label_index(g, st);
+        if (rc) return rc;
+    }
+    TRW_CUDA(cudaStreamSynchronize(st));
+    return TRW_OK;
+}
+
 int trw_graph_synchronize(trw_graph *g) {
     if (!g) return fail(TRW_ERR_INVALID, "null graph");
     TRW_CUDA(cudaSetDevice(g->device));

@@ -191,6 +191,14 @@ class Graph:
         N.check(_lib().trw_graph_indexes(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def build_indexes(self, edge_set: bool = True, label_index: bool = True, stream=None):
+        """Builds the Node2Vec edge set and / or the MetaPath label index now
+        (e.g. before serving) instead of in the first walk that needs them;
+        returns the states as indexes() does."""
+        N.check(_lib().trw_graph_build_indexes(self._h, 1 if edge_set else 0, 1 if label_index else 0,
+                                               ctypes.c_void_p(_stream_ptr(stream))))
+        return self.indexes()
+
     def device_error(self) -> int:
         c = ctypes.c_int32()
         N.check(_lib().trw_device_error(self._h, ctypes.byref(c)))
