@@ -161,6 +161,12 @@ public:
     int32_t degree(int32_t v) const { return degree_[v]; }
     trw_graph *handle() const { return h_.get(); }
 
+    // Builds the Node2Vec edge set and the MetaPath label index now instead
+    // of in the first walk that needs them (e.g. before timing or serving).
+    void build_indexes(bool edge_set = true, bool label_index = true) {
+        check(trw_graph_build_indexes(h_.get(), edge_set ? 1 : 0, label_index ? 1 : 0, nullptr));
+    }
+
 private:
     std::shared_ptr<trw_graph> h_;
     std::vector<int32_t> degree_;

@@ -1,6 +1,7 @@
 // Drives the C++ mirror of the reference interface (include/trw.hpp) the way
 // a ThunderRW app's execute() would: load the reference's CSR files, generate
-// walkers, compute<App>.  Prints steps and a checksum of every path.
+// walkers, compute<App>.  Prints steps and a checksum of every path.  A third
+// argument "prebuilt" builds the graph's lookup structures before the walk.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -13,6 +14,7 @@ int main(int argc, char **argv) {
     const std::string dir = argv[1];
     const std::string app = argv[2];
     trw::Graph graph = trw::Graph::load_csr(dir, /*edge_weight=*/true, /*edge_label=*/true);
+    if (argc > 3 && std::string(argv[3]) == "prebuilt") graph.build_indexes();  // before the first walk
     std::vector<trw::WalkerMeta> walkers;
     trw::generate_all_source(graph, walkers, /*shuffle=*/false);
     trw::Result r;

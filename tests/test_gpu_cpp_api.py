@@ -44,6 +44,8 @@ def test_cpp_compute_matches_oracle(exe, tmp_path, app, mode, sampler):
     g = G.make_graph("rmat", 1 << 10, 10, seed=13, labels=5)
     formats.store_csr(str(tmp_path), g["row"], g["adj"], weight=g["weight"], label=g["label"])
     out = subprocess.run([exe, str(tmp_path), app], check=True, capture_output=True, text=True).stdout.split()
+    pre = subprocess.run([exe, str(tmp_path), app, "prebuilt"], check=True, capture_output=True, text=True).stdout.split()
+    assert pre == out  # lookup structures built up front: the same walks
     og = O.Graph(g["row"], g["adj"], g["weight"], g["label"])
     if mode == "static":
         og.build_tables(sampler, 0)
