@@ -166,8 +166,9 @@ struct Scratch {
 /* How oracle_count_bytes charges the searches the GPU engine replaces with
  * lookups (bit flags; 0 = the reference's methods): 1 = Node2Vec's neighbour
  * test as one 32-byte probe of a hash set of the edges instead of the binary
- * search (graph.h:180-199); 2 = MetaPath's label row scan as one 32-byte read
- * of a label index's offsets. */
+ * search (graph.h:180-199); 2 = MetaPath's dynamic ITS from a label index:
+ * one 32-byte read of the wanted label's two CSR positions per step instead of
+ * the row pair and the label row scan. */
 static std::atomic<int> g_neighbor_accounting{0};
 
 extern "C" void oracle_set_neighbor_accounting(int32_t kind) { g_neighbor_accounting.store(kind); }
@@ -204,7 +205,14 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
         const int32_t cur = w.cur;
         const int64_t off = g->row[cur];
         const int32_t deg = (int32_t)(g->row[cur + 1] - off);
-        if (kCount) { bc->begin(); bc->touch(g->row + cur); }
+        if (kCount) {
+            bc->begin();
+            if (app.kind == APP_METAPATH && mode == MODE_DYNAMIC && sampler == S_ITS &&
+                (g_neighbor_accounting.load(std::memory_order_relaxed) & 2))
+                bc->bytes += 32;  /* a label index's two CSR positions of the wanted label, no row pair */
+            else
+                bc->touch(g->row + cur);
+        }
         if (deg == 0) break;  /* a sink: the reference divides by zero here */
         Cursor c(d->seed, wid, (uint32_t)w.len);
         int32_t nxt = -1;
@@ -295,9 +303,10 @@ void walk_one(const oracle_graph *g, const oracle_walk_desc *d, const App &app, 
             double *wt = sc.w.data();
             for (int32_t i = 0; i < deg; ++i) wt[i] = app.weight(g, w, g->adj[off + i], off + i);
             if (kCount) {
-                if (app.kind == APP_METAPATH && (g_neighbor_accounting.load(std::memory_order_relaxed) & 2))
-                    bc->bytes += 32;  /* the row's two label offsets of a label index */
-                else if (app.kind == APP_METAPATH) bc->span(g->label + off, (size_t)deg * 4);
+                if (app.kind == APP_METAPATH && sampler == S_ITS &&
+                    (g_neighbor_accounting.load(std::memory_order_relaxed) & 2)) {
+                    /* charged at the step's start */
+                } else if (app.kind == APP_METAPATH) bc->span(g->label + off, (size_t)deg * 4);
                 else if (app.kind == APP_DEEPWALK || app.kind == APP_GENERIC) bc->span(g->weight + off, (size_t)deg * 8);
                 else if (app.kind == APP_NODE2VEC) bc->span(g->adj + off, (size_t)deg * 4);
             }

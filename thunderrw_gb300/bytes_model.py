@@ -85,13 +85,12 @@ def metapath(paths: np.ndarray, row: np.ndarray, length: int) -> float:
 
 
 def metapath_index(paths: np.ndarray, row: np.ndarray, length: int) -> float:
-    """Bytes per move of MetaPath walks answered from the label index (a walk
-    that stops early is charged its last vertex's row pair, and its label
-    offsets when the row is not empty)."""
+    """Bytes per move of MetaPath walks answered from the label index: the
+    wanted label's two CSR positions, one sorted neighbour and the path
+    entry (no row pair; a walk that stops early is charged the positions
+    read at its last vertex)."""
     frm, to, k, p = _moves(paths)
     if frm.size == 0:
         return 0.0
-    row = np.asarray(row, dtype=np.int64)
     last = _stops(p, length)
-    tail = SECTOR * last.size + SECTOR * int((row[last + 1] > row[last]).sum())
-    return (frm.size * (SECTOR * 3 + 4) + tail) / frm.size
+    return (frm.size * (SECTOR * 2 + 4) + SECTOR * last.size) / frm.size

@@ -346,10 +346,10 @@ __global__ void build_label_index_kernel(const DevGraph g, int32_t K, int32_t *o
             if (lane >= o) x1 += y;
         }
         int32_t b0 = x0 - c0, b1 = total0 + x1 - c1;  // block starts of labels lane, lane + 32
-        int32_t *o = off + v * (int64_t)(K + 1);
-        if (lane < K) o[lane] = b0;
-        if (lane + 32 < K) o[lane + 32] = b1;
-        if (lane == 0) o[K] = r.y - r.x;
+        int32_t *o = off + v * (int64_t)(K + 1);  // absolute positions in nbr: a walk step needs no row pair
+        if (lane < K) o[lane] = r.x + b0;
+        if (lane + 32 < K) o[lane + 32] = r.x + b1;
+        if (lane == 0) o[K] = r.y;
         for (int32_t base = r.x; base < r.y; base += 32) {
             const int32_t i = base + lane;
             const int32_t lab = i < r.y ? __ldg(g.label + i) : -1;

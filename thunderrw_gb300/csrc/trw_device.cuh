@@ -102,8 +102,9 @@ struct DevGraph {
     // MetaPath's label index (built by the first MetaPath ITS walk when every
     // label lies in [0, lab_k), lab_k <= 64; null otherwise): lab_nbr holds
     // each row's neighbours stably sorted by edge label (row order inside a
-    // label), lab_off[v * (lab_k + 1) + l] the row-relative start of label l's
-    // block and lab_off[v * (lab_k + 1) + lab_k] the degree.
+    // label), lab_off[v * (lab_k + 1) + l] the position in lab_nbr where label
+    // l's block of row v starts and lab_off[v * (lab_k + 1) + lab_k] the row's
+    // end (lab_nbr is laid out like adj, so these are CSR positions).
     const int32_t *lab_nbr;
     const int32_t *lab_off;
     int32_t lab_k;

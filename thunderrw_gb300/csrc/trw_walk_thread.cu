@@ -164,7 +164,8 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
     for (int r = 0; r < R; ++r) {
         moved[r] = false;
         nxt[r] = 0;
-        if (s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
+        // the label index holds CSR positions itself: no row pair to read
+        if (S != kLabelIndex && s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
     }
     if (kSparse) {  // while the row pairs are in flight
 #pragma unroll
@@ -241,14 +242,15 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         // MetaPath's dynamic ITS over its 0/1 label weights (metapath.cpp:22-30,
         // inverse_transformation_sampling.h:288-313): the upper bound over the
         // 0/1 prefix sums picks match floor(count * real2) of the wanted label
-        // in row order, which the label index holds at lab_nbr[row + off[l] + m].
+        // in row order, which the label index holds at lab_nbr[off[l] + m]
+        // (an empty row or a label without match: the walker stops).
         int32_t lo[R], cnt[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             cnt[r] = 0;
             if (s[r].widx < 0) continue;
             const int32_t want = p.schema[(s[r].len - 1) % p.schema_len];
-            if (s[r].crow.y <= s[r].crow.x || want < 0 || want >= g.lab_k) continue;  // no match: the walker stops
+            if (want < 0 || want >= g.lab_k) continue;  // a label no edge has: no match
             const int32_t *off = g.lab_off + (int64_t)s[r].cur * (g.lab_k + 1) + want;
             lo[r] = __ldg(off);
             cnt[r] = __ldg(off + 1) - lo[r];
@@ -257,7 +259,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         for (int r = 0; r < R; ++r) {
             if (cnt[r] <= 0) continue;
             const int32_t m = (int32_t)((double)cnt[r] * real2(rnd[r].x));  // floor of P[last] * dr_
-            nxt[r] = __ldg(g.lab_nbr + s[r].crow.x + lo[r] + m);
+            nxt[r] = __ldg(g.lab_nbr + lo[r] + m);
             moved[r] = true;
         }
     } else if (S == kRejection) {
@@ -325,7 +327,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         if (s[r].widx < 0) continue;
         if (!moved[r]) { finish(p, s[r]); continue; }
         s[r].prev = s[r].cur;
-        s[r].prow = s[r].crow;
+        if (S != kLabelIndex) s[r].prow = s[r].crow;  // (the label index reads no row pair)
         s[r].cur = nxt[r];
         if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
         s[r].len += 1;
