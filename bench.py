@@ -193,8 +193,9 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
             total_t += time.perf_counter() - t0
             total_steps += r["steps"]
             done_q += qs.size
-        sample = "%d queries x %d walkers (%d steps, %.2f passes over the batch) in %.1f s" % (
-            done_q, per_query, total_steps, done_q / src.size, total_t)
+        sample = ("step-interleaved C++ port of the reference ring (64 walkers per thread), "
+                  "%d queries x %d walkers (%d steps, %.2f passes over the batch) in %.1f s" % (
+                      done_q, per_query, total_steps, done_q / src.size, total_t))
         return total_steps / total_t, sample, ncores
     if wl_name == "deepwalk":
         og.build_tables("alias", 0)
@@ -220,8 +221,10 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
         done += s.size
         paths = r["paths"]
     del paths
-    return total_steps / total_t, "%d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
-        done, wl["length"] - 1, total_steps, done / src.size, total_t), ncores
+    form = ("step-interleaved C++ port of the reference ring (64 walkers per thread)" if interleaved
+            else "C++ port of the reference's per-walker moves")
+    return total_steps / total_t, "%s, %d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
+        form, done, wl["length"] - 1, total_steps, done / src.size, total_t), ncores
 
 
 # ---------------------------------------------------------------------------
@@ -239,6 +242,7 @@ def run_reference(args):
     row = inp["row"].cpu().numpy()
     adj = inp["adj"].cpu().numpy()
     weight = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
+    label = inp["label"].cpu().numpy() if inp.get("label") is not None else None
     src = inp["sources"].cpu().numpy()
     per_q = inp.get("per_query", 0)
     del inp
@@ -249,7 +253,7 @@ def run_reference(args):
     cores = os.cpu_count()
     for i in range(args.warmup + args.steps):
         v, sample, cores = cpu_baseline(args.workload, wl, row, adj, weight, src, per_q,
-                                        max(2.0, 20.0 / max(1, args.warmup + args.steps)), 0)
+                                        max(2.0, 20.0 / max(1, args.warmup + args.steps)), 0, label=label)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
@@ -259,8 +263,7 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
         "config": {"workload": workload_name(wl, args)},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": "step-interleaved C++ port of the reference ring (64 walkers per thread), "
-                                   "per step " + sample},
+                         "sample": "per step: " + sample},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -542,8 +545,7 @@ def run_ours(args):
         lab = inp["label"].cpu().numpy() if inp.get("label") is not None else None
         v, sample, cores = cpu_baseline(args.workload, wl, row, adj, wt, src.cpu().numpy(),
                                         inp.get("per_query", 0), args.cpu_seconds, 0, label=lab)
-        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port",
-               "sample": "step-interleaved C++ port of the reference ring, " + sample}
+        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
 
     if rank == 0:
         line = {
