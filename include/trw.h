@@ -175,7 +175,10 @@ int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t o
  *                   added to, not overwritten
  *   steps           receives the number of moves (creeper.h:305), or NULL
  * Walkers at a vertex without neighbours stop (the reference divides by zero
- * there). */
+ * there).  With host paths / lengths and at least four walkers per lane of
+ * the GPU (SMs x 2048), the walkers run as up to 16 ranges whose outputs are
+ * copied back while the next range walks; the results are those of one
+ * launch. */
 int trw_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_walkers,
              int64_t id_base, int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts,
              uint64_t *steps, int32_t engine, trw_stream_t stream);
@@ -200,8 +203,11 @@ int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *source
  * depends on the counts alone (not on scheduling).  offsets has
  * num_queries + 1 entries; vertices and counts hold `capacity` entries.  If
  * the batch needs more than `capacity` entries, offsets is still written
- * (offsets[num_queries] is the size needed), no entry is written, and the
- * call reports TRW_ERR_CAPACITY (synchronous calls) or device error 4. */
+ * (offsets[num_queries] is the size needed), only the queries whose entries
+ * end within `capacity` are written, and the call reports TRW_ERR_CAPACITY
+ * (synchronous calls) or device error 4.  With host outputs a large batch
+ * runs as several ranges of queries whose entries are copied back while the
+ * next range walks; the output is that of one range. */
 int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
                          int64_t walkers_per_query, int64_t *offsets, int32_t *vertices, int32_t *counts,
                          int64_t capacity, uint64_t *steps, int32_t engine, trw_stream_t stream);
