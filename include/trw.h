@@ -203,9 +203,11 @@ int trw_ppr_batch(trw_graph *g, const trw_walk_desc *desc, const int32_t *source
  * depends on the counts alone (not on scheduling).  offsets has
  * num_queries + 1 entries; vertices and counts hold `capacity` entries.  If
  * the batch needs more than `capacity` entries, offsets is still written
- * (offsets[num_queries] is the size needed), only the queries whose entries
- * end within `capacity` are written, and the call reports TRW_ERR_CAPACITY
- * (synchronous calls) or device error 4.  With host outputs a large batch
+ * (offsets[num_queries] is the size needed), at most the queries whose
+ * entries end within `capacity` are written (with host outputs, only whole
+ * query ranges that do), and the call reports TRW_ERR_CAPACITY (synchronous
+ * calls) or device error 4: grow the buffers to offsets[num_queries] and
+ * call again.  With host outputs a large batch
  * runs as several ranges of queries whose entries are copied back while the
  * next range walks; the output is that of one range. */
 int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_queries,
