@@ -200,11 +200,9 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
     if wl_name == "deepwalk":
         og.build_tables("alias", 0)
         d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=11)
-        interleaved = True
-    else:  # dynamic samplers: the plain per-walker port on all threads
+    else:  # dynamic samplers, on the same step-interleaved ring
         d = O.make_desc(wl_name, "dynamic", "maxweight_rejection" if wl_name == "node2vec" else "its",
                         length=wl["length"], p=wl.get("p", 1.0), q=wl.get("q", 1.0), schema=wl.get("schema"), seed=11)
-        interleaved = False
     src = np.asarray(sources, dtype=np.int32)
     total_steps, total_t, done = 0, 0.0, 0
     chunk = 1 << 16
@@ -215,14 +213,13 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
         at = done % src.size
         s = src[at:at + chunk]
         t0 = time.perf_counter()
-        r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=interleaved, ring=64)
+        r = O.walk(og, d, s, id_base=done, path_cap=wl["length"], threads=ncores, interleaved=True, ring=64)
         total_t += time.perf_counter() - t0
         total_steps += r["steps"]
         done += s.size
         paths = r["paths"]
     del paths
-    form = ("step-interleaved C++ port of the reference ring (64 walkers per thread)" if interleaved
-            else "C++ port of the reference's per-walker moves")
+    form = "step-interleaved C++ port of the reference ring (64 walkers per thread)"
     return total_steps / total_t, "%s, %d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
         form, done, wl["length"] - 1, total_steps, done / src.size, total_t), ncores
 

@@ -536,8 +536,14 @@ int oracle_count_bytes(const oracle_graph *g, const oracle_walk_desc *d, const i
  * stages of every occupied slot before the next stage, issuing prefetches for
  * the next stage's random access (creeper.h:387-399 with
  * uniform_interleaving_move uniform_sampling.h:11-45 and
- * static_alias_interleaving_move alias_sampling.h:221-258).  Admission and
- * update follow creeper.h:299-334. */
+ * static_alias_interleaving_move alias_sampling.h:221-258; for dynamic mode
+ * the ring of creeper.h:543-687: max-weight rejection's first trial
+ * position drawn and its neighbour prefetched a stage ahead, as MaxRSFrame
+ * does, rs_frame.h:47-83, later trials in place; dynamic ITS with the row
+ * pair prefetched and the gather, prefix and search of
+ * dynamic_its_interleaving_move in place).  Admission and update follow
+ * creeper.h:299-334.  Draws are consumed in the order of walk_one, so the
+ * walks are the same. */
 int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
                             const int32_t *sources, int64_t num_walkers, int64_t per_query,
                             int64_t id_base, int32_t *paths, int32_t path_cap,
@@ -546,17 +552,25 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
     int rc = validate(g, d);
     if (rc) return rc;
     const bool uniform = d->mode == MODE_UNIFORM;
-    if (!uniform && !(d->mode == MODE_STATIC && d->sampler == S_ALIAS)) return -2;
+    const bool alias = d->mode == MODE_STATIC && d->sampler == S_ALIAS;
+    const bool maxrs = d->mode == MODE_DYNAMIC && d->sampler == S_MAXRS;
+    const bool dits = d->mode == MODE_DYNAMIC && d->sampler == S_ITS;
+    if (!uniform && !alias && !maxrs && !dits) return -2;
     if (ring <= 0) ring = 64;
     const App app(d);
+    const double maxw = app.max_weight();
     const int32_t nt = nthreads(threads);
     std::vector<uint64_t> tsteps(nt, 0);
     /* static walker chunks per thread, as creeper.h:729-734 */
     auto body = [&](int tid) {
         int64_t chunk = num_walkers / nt;
         int64_t b = tid * chunk, e = tid == nt - 1 ? num_walkers : b + chunk;
-        struct Slot { bool empty; int64_t idx; Walker w; int64_t pos; int64_t off; int32_t deg; uint32_t u0, u1; };
+        struct Slot {
+            bool empty; int64_t idx; Walker w; int64_t pos; int64_t off; int32_t deg; uint32_t u0, u1;
+            Cursor c{0, 0, 0};  /* the move's draws (dynamic mode) */
+        };
         std::vector<Slot> r(ring);
+        std::vector<double> wt;  /* dynamic ITS: the gathered row */
         int64_t next = b;
         uint64_t st = 0;
         auto admit = [&](Slot &s) {
@@ -579,8 +593,8 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
         while (active > 0) {
             /* stage 1: draw and prefetch the row pair */
             for (auto &s : r) if (!s.empty) {
-                Cursor c(d->seed, (uint64_t)(id_base + s.idx), (uint32_t)s.w.len);
-                s.u0 = c.u32(); s.u1 = c.u32();
+                s.c = Cursor(d->seed, (uint64_t)(id_base + s.idx), (uint32_t)s.w.len);
+                if (uniform || alias) { s.u0 = s.c.u32(); s.u1 = s.c.u32(); }
                 __builtin_prefetch(g->row + s.w.cur);
             }
             /* stage 2: position and prefetch of the adjacency entry / alias slot */
@@ -588,8 +602,16 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
                 s.off = g->row[s.w.cur];
                 s.deg = (int32_t)(g->row[s.w.cur + 1] - s.off);
                 if (s.deg == 0) continue;
-                s.pos = s.off + (s.u0 % (uint32_t)s.deg);
-                if (uniform) __builtin_prefetch(g->adj + s.pos); else __builtin_prefetch(g->alias + s.pos);
+                if (maxrs) {  /* the first trial's position */
+                    s.pos = s.off + (s.c.u32() % (uint32_t)s.deg);
+                    __builtin_prefetch(g->adj + s.pos);
+                } else if (dits) {
+                    __builtin_prefetch(d->app == APP_METAPATH ? (const void *)(g->label + s.off)
+                                                              : (const void *)(g->weight + s.off));
+                } else {
+                    s.pos = s.off + (s.u0 % (uint32_t)s.deg);
+                    if (uniform) __builtin_prefetch(g->adj + s.pos); else __builtin_prefetch(g->alias + s.pos);
+                }
             }
             /* stage 3: move, then update and refill */
             for (auto &s : r) if (!s.empty) {
@@ -597,9 +619,33 @@ int oracle_walk_interleaved(const oracle_graph *g, const oracle_walk_desc *d,
                 if (s.deg == 0) {
                     done = true;
                 } else {
-                    int32_t nxt;
+                    int32_t nxt = -1;
+                    bool stop = false;
                     if (uniform) nxt = g->adj[s.pos];
-                    else { const oracle_alias_slot &a = g->alias[s.pos]; nxt = real2(s.u1) <= a.prob ? a.first : a.second; }
+                    else if (alias) { const oracle_alias_slot &a = g->alias[s.pos]; nxt = real2(s.u1) <= a.prob ? a.first : a.second; }
+                    else if (maxrs) {  /* dynamic_max_weight_rs_move's trials (rejection_sampling.h:368-402) */
+                        int64_t t = 0;
+                        int64_t pos = s.pos;
+                        double sel = app.weight(g, s.w, g->adj[pos], pos);
+                        double rr = real2(s.c.u32()) * maxw;
+                        while (rr > sel && ++t < kMaxTrials) {
+                            pos = s.off + (s.c.u32() % (uint32_t)s.deg);
+                            sel = app.weight(g, s.w, g->adj[pos], pos);
+                            rr = real2(s.c.u32()) * maxw;
+                        }
+                        if (t >= kMaxTrials) stop = true;
+                        else nxt = g->adj[pos];
+                    } else {  /* dynamic ITS: gather, prefix, search (inverse_transformation_sampling.h:288-313) */
+                        if ((int32_t)wt.size() < s.deg) wt.resize(s.deg);
+                        for (int32_t i = 0; i < s.deg; ++i) wt[i] = app.weight(g, s.w, g->adj[s.off + i], s.off + i);
+                        for (int32_t x = 1; x < s.deg; ++x) wt[x] += wt[x - 1];
+                        if (wt[s.deg - 1] == 0.0) stop = true;
+                        else {
+                            const double target = real2(s.c.u32()) * wt[s.deg - 1];
+                            nxt = g->adj[s.off + upper_bound_bl(wt.data(), s.deg, target)];
+                        }
+                    }
+                    if (stop) { finish(s); active -= 1; admit(s); active += !s.empty; continue; }
                     s.w.prev = s.w.cur; s.w.cur = nxt;
                     if (paths && s.w.len < path_cap) paths[(size_t)s.idx * path_cap + s.w.len] = nxt;
                     s.w.len += 1;

@@ -45,9 +45,11 @@ def test_oracle_matches_reference(case):
 
 
 @pytest.mark.parametrize("case", [c for c in CASES if (c["mode"], c["sampler"]) in
-                                  (("uniform", "uniform"), ("static", "alias"))], ids=case_id)
+                                  (("uniform", "uniform"), ("static", "alias"), ("dynamic", "maxweight_rejection"),
+                                   ("dynamic", "its"))], ids=case_id)
 def test_interleaved_ring_matches(case):
-    """The step-interleaved oracle (timed CPU baseline) walks identically."""
+    """The step-interleaved oracle (timed CPU baseline) walks identically,
+    dynamic max-weight rejection and dynamic ITS included."""
     g = _oracle_graph(case)
     if case["mode"] == "static":
         g.build_tables("alias", 1 if case["app"] == "ppr" else 0)
