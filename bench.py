@@ -6,17 +6,26 @@ Default workload (the batched-PPR configuration): R-MAT graph (a,b,c =
 undirected int32 CSR; 4096 queries x 10^4 walkers whose sources are drawn
 uniformly among non-isolated vertices; uniform sampling, termination
 probability 0.2 after every move (geometric lengths, mean 5); output: int32
-visit counts per query (4096 x N, zeroed inside every step).  One step = one
-whole batch through trw_ppr_batch.  Inputs (adjacency 0.5 GB, counts 64 GiB)
-are far larger than the 129 MB L2, so no separate flush is needed.
+visit counts per query as sparse CSR (offsets, vertex, count).  One step =
+one whole batch through trw_ppr_batch_sparse.  Inputs (adjacency 0.5 GB,
+per-query tables 2 GiB) are far larger than the 129 MB L2, so no separate
+flush is needed.
+
+After the headline workload the default run measures the other single-GPU
+workloads for a few steps each (``workloads`` key): DeepWalk static alias
+(Chung-Lu 2^18), Node2Vec max-weight rejection (R-MAT 2^24) and MetaPath
+dynamic ITS (R-MAT 2^24).  Every workload's last timed batch is checked
+against the CPU oracle on a sample, outside the timed region
+(``parity_checked``).
 
 Prints one JSON line (rank 0).  --impl reference times the reference's CPU
 algorithm (the step-interleaved C++ oracle port of creeper.h's ring) on the
-host cores instead.
+host cores instead, with the same ``config``.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -24,6 +33,7 @@ import subprocess
 import sys
 import threading
 import time
+from types import SimpleNamespace
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -41,6 +51,20 @@ BYTES_PER_STEP = {
     "deepwalk": bytes_model.STATIC_ALIAS,
 }
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per step of each
+# workload's walk kernel, from one ncu capture of that kernel: PPR on the
+# full N = 2^22 graph with 256 queries (the full batch's tables do not change
+# the per-step traffic of the walk: only the in-flight queries' tables are
+# written), the others on their full graphs with a reduced walker count.
+# Scaled by the steps of one full launch.
+TRAFFIC_BYTES_PER_STEP = {
+    "ppr": 70.73,
+    "ppr_dense": 89.13,
+    "deepwalk": 16.47,
+    "node2vec": 274.7,
+    "metapath": 155.1,
+}
+
 WORKLOADS = {
     "ppr": dict(kind="rmat", n=1 << 22, deg=32, queries=4096, per_query=10_000, tp=0.2,
                 name="ppr_batch rmat(0.57,0.19,0.19) N=2^22 deg=32 undirected, 4096 queries x 1e4 walkers, "
@@ -53,6 +77,8 @@ WORKLOADS = {
     "metapath": dict(kind="rmat", n=1 << 24, deg=32, length=20, walkers=1 << 22, labels=5, schema=[0, 1, 2, 3, 4],
                      name="metapath schema 0..4 dynamic ITS rmat N=2^24 deg=32, 5 labels, 2^22 random sources, L=20"),
 }
+SIDE_WORKLOADS = ("deepwalk", "node2vec", "metapath")
+L2_BYTES = 129e6
 
 
 def parse():
@@ -69,6 +95,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="keep the automatic launch shape (no autotuning)")
+    ap.add_argument("--no-workloads", action="store_true", help="measure the headline workload only")
+    ap.add_argument("--no-parity", action="store_true", help="skip the untimed oracle check of a timed batch")
+    ap.add_argument("--side-steps", type=int, default=5, help="timed steps of each side workload")
     ap.add_argument("--shape", default=None, help="walkers_per_lane,ctas_per_sm: set this launch shape, no tuning")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--dense", action="store_true", help="PPR: dense Q x N count output instead of sparse CSR")
@@ -136,29 +165,53 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# workload construction
+# workload construction and description (shared by both arms)
 # ---------------------------------------------------------------------------
 
-def workload_name(wl, args):
+def workload_name(wl, over):
     """The workload's name, with any size override spelled out."""
-    over = []
-    if args.scale:
-        over.append("N=2^%d" % args.scale)
-    if args.queries:
-        over.append("%d queries" % args.queries)
-    return wl["name"] + (" [reduced: %s]" % ", ".join(over) if over else "")
+    extra = []
+    if over.scale:
+        extra.append("N=2^%d" % over.scale)
+    if over.queries:
+        extra.append("%d queries" % over.queries)
+    return wl["name"] + (" [reduced: %s]" % ", ".join(extra) if extra else "")
 
 
-def build_inputs(wl, args, device, rank=0):
+def needs_l2_flush(name, n, e):
+    """Working sets that fit in the 129 MB L2 are flushed between timed steps."""
+    working = e * 4 + n * 8 + (e * 16 if name == "deepwalk" else 0)
+    return working < 2 * L2_BYTES
+
+
+def workload_config(name, wl, over, n, e, walkers):
+    """The ``config`` of the JSON line: the same dict in both arms."""
+    cfg = {"workload": workload_name(wl, over), "n": int(n), "e": int(e)}
+    if "queries" in wl:
+        q = over.queries or wl["queries"]
+        # every visited vertex has a neighbour (undirected graph, non-isolated
+        # sources), so a walker makes 1/tp moves on average
+        cfg.update(queries=q, walkers_per_query=wl["per_query"], tp=wl["tp"],
+                   steps_per_batch=int(round(q * wl["per_query"] / wl["tp"])))
+    else:
+        cfg.update(walkers=int(walkers), length=wl["length"])
+        if name in ("deepwalk", "node2vec"):  # no dead ends: every walker makes L - 1 moves
+            cfg["steps_per_batch"] = int(walkers) * (wl["length"] - 1)
+    cfg["l2"] = ("L2 flushed between timed steps (512 MB write outside the events)" if needs_l2_flush(name, n, e)
+                 else "inputs larger than L2 (adjacency %.2f GB), no flush" % (e * 4 / 1e9))
+    return cfg
+
+
+def build_inputs(wl, over, device, rank=0):
     """The workload's graph (the same on every rank) and rank's own sources."""
     import torch
     from thunderrw_gb300 import generators as G
-    n = 1 << args.scale if args.scale else wl["n"]
+    n = 1 << over.scale if over.scale else wl["n"]
     g = G.make_graph(wl["kind"], n, wl["deg"], seed=20240601, device=device,
                      weights=wl["kind"] != "rmat" or "length" in wl, labels=wl.get("labels", 0))
     out = {"n": n, "row": g["row"], "adj": g["adj"], "weight": g["weight"], "label": g["label"]}
     if "queries" in wl:
-        q = args.queries or wl["queries"]
+        q = over.queries or wl["queries"]
         out["sources"] = G.random_sources(g["row"], q, seed=replicas.replica_seed(7, rank) & 0x7FFFFFFF)
         out["per_query"] = wl["per_query"]
     elif "walkers" in wl:
@@ -170,43 +223,64 @@ def build_inputs(wl, args, device, rank=0):
     return out
 
 
-def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, threads, label=None):
+def host_arrays(inp):
+    def h(k):
+        return inp[k].cpu().numpy() if inp.get(k) is not None else None
+    return {k: h(k) for k in ("row", "adj", "weight", "label", "sources")}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the step-interleaved port of the reference ring
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(name, wl, host, per_query, seconds, threads=0):
     """The step-interleaved CPU port (oracle) on a bounded sample of the same
-    workload, on all host threads.  Returns (steps/s, sample description)."""
+    workload, on all host threads.  Returns a dict (value, sample, cores, ...).
+
+    PPR: the reference's PPR app counts nothing (ppr.cpp:27-29), so the
+    headline value is the count-free walk; the same walks recording visit
+    counts into a dense per-query block are timed too (``value_with_counts``),
+    with the block zeroed outside the timed passes."""
     from oracle import oracle as O
-    og = O.Graph(row, adj, weight, label)
+    og = O.Graph(host["row"], host["adj"], host["weight"], host["label"])
     ncores = threads or os.cpu_count()
-    if wl_name == "ppr":
+    src = np.asarray(host["sources"], dtype=np.int32)
+    form = "step-interleaved C++ port of the reference ring (64 walkers per thread)"
+    if name == "ppr":
         d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=wl["tp"], seed=11)
-        chunk = 64  # queries per pass; each pass zeroes and fills a chunk x N count block
+        chunk = 64  # queries per pass
         counts = np.zeros((chunk, og.n), dtype=np.int32)
-        counts.fill(1)  # touch every page once, outside the timed passes
-        total_steps, total_t, done_q = 0, 0.0, 0
-        src = np.asarray(sources, dtype=np.int32)
-        while total_t < seconds:  # the batch again (fresh walker ids) until the budget is spent
-            at = done_q % src.size
-            qs = src[at:at + chunk]
-            t0 = time.perf_counter()
-            counts[: qs.size].fill(0)
-            r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_lengths=False,
-                       num_queries=qs.size, threads=ncores, interleaved=True, ring=64, out_counts=counts)
-            total_t += time.perf_counter() - t0
-            total_steps += r["steps"]
-            done_q += qs.size
-        sample = ("step-interleaved C++ port of the reference ring (64 walkers per thread), "
-                  "%d queries x %d walkers (%d steps, %.2f passes over the batch) in %.1f s" % (
-                      done_q, per_query, total_steps, done_q / src.size, total_t))
-        return total_steps / total_t, sample, ncores
-    if wl_name == "deepwalk":
+        res = {}
+        for with_counts in (False, True):
+            total_steps, total_t, done_q = 0, 0.0, 0
+            budget = seconds / 2
+            while total_t < budget:  # the batch again (fresh walker ids) until the budget is spent
+                at = done_q % src.size
+                qs = src[at:at + chunk]
+                if with_counts:
+                    counts[: qs.size].fill(0)  # outside the timed pass
+                t0 = time.perf_counter()
+                r = O.walk(og, d, qs, per_query=per_query, id_base=done_q * per_query, want_lengths=False,
+                           num_queries=qs.size, threads=ncores, interleaved=True, ring=64,
+                           out_counts=counts if with_counts else None)
+                total_t += time.perf_counter() - t0
+                total_steps += r["steps"]
+                done_q += qs.size
+            res[with_counts] = (total_steps / total_t, done_q, total_steps, total_t)
+        v, dq, st, tt = res[False]
+        vc, dqc, stc, ttc = res[True]
+        sample = ("%s, count-free as the reference's PPR: %d queries x %d walkers (%d steps, %.2f passes over the "
+                  "batch) in %.1f s; with dense visit counts (block zeroed outside the timed passes): %d queries, "
+                  "%d steps in %.1f s" % (form, dq, per_query, st, dq / src.size, tt, dqc, stc, ttc))
+        return {"value": v, "value_with_counts": vc, "sample": sample, "cores": ncores}
+    if name == "deepwalk":
         og.build_tables("alias", 0)
         d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=11)
     else:  # dynamic samplers, on the same step-interleaved ring
-        d = O.make_desc(wl_name, "dynamic", "maxweight_rejection" if wl_name == "node2vec" else "its",
+        d = O.make_desc(name, "dynamic", "maxweight_rejection" if name == "node2vec" else "its",
                         length=wl["length"], p=wl.get("p", 1.0), q=wl.get("q", 1.0), schema=wl.get("schema"), seed=11)
-    src = np.asarray(sources, dtype=np.int32)
     total_steps, total_t, done = 0, 0.0, 0
     chunk = 1 << 16
-    paths = None
     # chunks of the workload's walkers in order; a workload that finishes
     # before the time budget runs again (fresh walker ids) until it is spent
     while total_t < seconds:
@@ -217,11 +291,10 @@ def cpu_baseline(wl_name, wl, row, adj, weight, sources, per_query, seconds, thr
         total_t += time.perf_counter() - t0
         total_steps += r["steps"]
         done += s.size
-        paths = r["paths"]
-    del paths
-    form = "step-interleaved C++ port of the reference ring (64 walkers per thread)"
-    return total_steps / total_t, "%s, %d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
-        form, done, wl["length"] - 1, total_steps, done / src.size, total_t), ncores
+        del r
+    sample = "%s, %d walkers x %d steps (%d steps, %.2f passes over the workload) in %.1f s" % (
+        form, done, wl["length"] - 1, total_steps, done / src.size, total_t)
+    return {"value": total_steps / total_t, "sample": sample, "cores": ncores}
 
 
 # ---------------------------------------------------------------------------
@@ -236,31 +309,31 @@ def run_reference(args):
     wl = WORKLOADS[args.workload]
     have_gpu = torch.cuda.is_available()
     inp = build_inputs(wl, args, "cuda" if have_gpu else "cpu")
-    row = inp["row"].cpu().numpy()
-    adj = inp["adj"].cpu().numpy()
-    weight = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
-    label = inp["label"].cpu().numpy() if inp.get("label") is not None else None
-    src = inp["sources"].cpu().numpy()
+    host = host_arrays(inp)
+    n, e = inp["n"], int(inp["adj"].numel())
     per_q = inp.get("per_query", 0)
     del inp
     if have_gpu:
         torch.cuda.empty_cache()
-    vals = []
-    sample = ""
-    cores = os.cpu_count()
+    vals, vals_c = [], []
+    res = {}
     for i in range(args.warmup + args.steps):
-        v, sample, cores = cpu_baseline(args.workload, wl, row, adj, weight, src, per_q,
-                                        max(2.0, 20.0 / max(1, args.warmup + args.steps)), 0, label=label)
+        res = cpu_baseline(args.workload, wl, host, per_q, max(2.0, 20.0 / max(1, args.warmup + args.steps)))
         if i >= args.warmup:
-            vals.append(v)
+            vals.append(res["value"])
+            if "value_with_counts" in res:
+                vals_c.append(res["value_with_counts"])
     value = statistics.median(vals)
+    cpu = {"value": value, "unit": "steps/s", "cores": res["cores"], "kind": "port",
+           "sample": "per step: " + res["sample"]}
+    if vals_c:
+        cpu["value_with_counts"] = statistics.median(vals_c)
     line = {
         "impl": "reference", "metric": "walk_steps_per_s", "value": value, "unit": "steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
-        "config": {"workload": workload_name(wl, args)},
-        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
-                         "sample": "per step: " + sample},
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded generator, no dataset)",
+        "config": workload_config(args.workload, wl, args, n, e, host["sources"].size),
+        "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -271,32 +344,71 @@ def run_reference(args):
 # our arm
 # ---------------------------------------------------------------------------
 
-def run_ours(args):
-    import torch
-    import torch.distributed as dist
+def _c(t):
+    return ctypes.c_void_p(t.data_ptr())
 
-    rank, world, local = dist_env()
-    if world > 1:
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
+
+def parity_sample(name, wl, host, seed, out, per_query):
+    """Checks a sample of one timed batch against the CPU oracle, bit for
+    bit: the first 8 queries' (vertex, count) lists of a PPR batch, or the
+    paths and lengths of the first 2^14 walkers of a walk batch."""
+    from oracle import oracle as O
+    og = O.Graph(host["row"], host["adj"], host["weight"], host["label"])
+    src = host["sources"]
+    if name == "ppr":
+        nq = min(8, src.size)
+        d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=wl["tp"], seed=seed)
+        ref = O.walk(og, d, src[:nq], per_query=per_query, want_counts=True, want_lengths=False)
+        off, vert, cnt = out
+        off = off[: nq + 1].cpu().numpy()
+        vert = vert[: off[-1]].cpu().numpy()
+        cnt = cnt[: off[-1]].cpu().numpy()
+        for q in range(nq):
+            v, c = vert[off[q]:off[q + 1]], cnt[off[q]:off[q + 1]]
+            nz = np.nonzero(ref["counts"][q])[0]
+            order = np.argsort(v)
+            if v.size != nz.size or not np.array_equal(v[order], nz) or not np.array_equal(c[order], ref["counts"][q][nz]):
+                return False, "query %d differs from the oracle" % q
+        return True, "first %d queries' (vertex, count) lists == oracle (%d steps)" % (nq, ref["steps"])
+    k = min(src.size, 1 << 14)
+    if name == "deepwalk":
+        og.build_tables("alias", 0)
+        d = O.make_desc("deepwalk", "static", "alias", length=wl["length"], seed=seed)
+    else:
+        d = O.make_desc(name, "dynamic", "maxweight_rejection" if name == "node2vec" else "its",
+                        length=wl["length"], p=wl.get("p", 1.0), q=wl.get("q", 1.0), schema=wl.get("schema"),
+                        seed=seed)
+    ref = O.walk(og, d, src[:k], path_cap=wl["length"])
+    paths, lengths = out
+    ok = np.array_equal(paths[:k].cpu().numpy(), ref["paths"]) and np.array_equal(lengths[:k].cpu().numpy(),
+                                                                                   ref["lengths"])
+    return ok, "first %d walkers' paths and lengths %s oracle (%d steps)" % (k, "==" if ok else "!=", ref["steps"])
+
+
+def measure(name, args, over, dev, rank, world, steps, warmup, headline):
+    """Times one workload through the C ABI; returns its result dict."""
+    import torch
     from thunderrw_gb300 import _native as N
     from thunderrw_gb300 import engine as E
 
-    wl = WORKLOADS[args.workload]
-    inp = build_inputs(wl, args, dev, rank)
+    wl = WORKLOADS[name]
+    t_build = time.perf_counter()
+    inp = build_inputs(wl, over, dev, rank)
     graph = E.Graph(inp["row"], inp["adj"], inp["weight"], inp.get("label"))
+    build_s = time.perf_counter() - t_build
     stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
     L = N.load()
-    import ctypes
+    res = {"config": workload_config(name, wl, over, graph.n, graph.e, inp["sources"].numel()),
+           "graph_build_s": build_s}
 
-    sparse = args.workload == "ppr" and not args.dense
-    out_bytes = 0
-    if args.workload == "ppr":
-        Q = inp["sources"].numel()
+    sparse = name == "ppr" and not args.dense
+    src = inp["sources"]
+    steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
+    counts = None
+    if name == "ppr":
+        Q = src.numel()
         per_q = inp["per_query"]
-        steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
-        src = inp["sources"]
         if sparse:
             # size the CSR output from one untimed batch (same shape, other seed)
             probe = E.ppr_batch_sparse(graph, src, per_q, tp=wl["tp"], seed=999)
@@ -305,84 +417,82 @@ def run_ours(args):
             offsets = torch.empty(Q + 1, dtype=torch.int64, device=dev)
             vert = torch.empty(cap, dtype=torch.int32, device=dev)
             vcnt = torch.empty(cap, dtype=torch.int32, device=dev)
-            counts = None
+            outputs = (offsets, vert, vcnt)
 
             def one_step(seed, engine="persistent"):
                 d = E.PPR(wl["tp"]).desc(replicas.replica_seed(seed, rank))
-                N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q,
-                                               per_q, ctypes.c_void_p(offsets.data_ptr()),
-                                               ctypes.c_void_p(vert.data_ptr()), ctypes.c_void_p(vcnt.data_ptr()), cap,
-                                               ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
-                                               ctypes.c_void_p(stream.cuda_stream)))
+                N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), _c(src), Q, per_q, _c(offsets),
+                                               _c(vert), _c(vcnt), cap, _c(steps_dev), N.ENGINES[engine], sp))
+            # walk, distinct, segment scan, offsets scan, emit (one query range)
+            launches_per_step = 5
         else:
             counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
+            outputs = None
 
             def one_step(seed, engine="persistent"):
                 d = E.PPR(wl["tp"]).desc(replicas.replica_seed(seed, rank))
-                N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), Q, per_q,
-                                        ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(steps_dev.data_ptr()),
-                                        1, N.ENGINES[engine], ctypes.c_void_p(stream.cuda_stream)))
+                N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), _c(src), Q, per_q, _c(counts),
+                                        _c(steps_dev), 1, N.ENGINES[engine], sp))
+            launches_per_step = 1
+        app = E.PPR(wl["tp"])
     else:
-        src = inp["sources"]
         W = src.numel()
         Lw = wl["length"]
         paths = torch.empty((W, Lw), dtype=torch.int32, device=dev)
         lengths = torch.empty(W, dtype=torch.int32, device=dev)
-        steps_dev = torch.zeros(1, dtype=torch.int64, device=dev)
-        counts = None
+        outputs = (paths, lengths)
         app = {"deepwalk": E.DeepWalk(Lw),
                "node2vec": E.Node2Vec(Lw, wl.get("p", 2.0), wl.get("q", 0.5)),
-               "metapath": E.MetaPath(Lw, wl.get("schema", [0, 1, 2, 3, 4]))}[args.workload]
-        if args.workload == "deepwalk":
+               "metapath": E.MetaPath(Lw, wl.get("schema", [0, 1, 2, 3, 4]))}[name]
+        if name == "deepwalk":
             graph.build_tables("alias", "edge")
 
         def one_step(seed, engine="persistent"):
             d = app.desc(replicas.replica_seed(seed, rank))
-            N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(src.data_ptr()), W, 0,
-                               ctypes.c_void_p(paths.data_ptr()), Lw, ctypes.c_void_p(lengths.data_ptr()), None,
-                               ctypes.c_void_p(steps_dev.data_ptr()), N.ENGINES[engine],
-                               ctypes.c_void_p(stream.cuda_stream)))
+            N.check(L.trw_walk(graph.handle, ctypes.byref(d), _c(src), W, 0, _c(paths), Lw, _c(lengths), None,
+                               _c(steps_dev), N.ENGINES[engine], sp))
+        launches_per_step = 1
 
     # ---- launch shape: tuned once on a sample of this workload, as a user
     # would (thunderrw_gb300/autotune.py), outside every timed region
-    shape = None
-    if args.shape:
-        slot = "uniform" if args.workload == "ppr" else app.sampler
+    shape = "automatic"
+    if args.shape and headline:
+        slot = "uniform" if name == "ppr" else app.sampler
         r, c = (int(x) for x in args.shape.split(","))
         graph.set_engine_shape(slot, r, c)
         shape = {"slot": slot, "walkers_per_lane": r, "ctas_per_sm": c, "set_by": "--shape"}
     elif not args.no_tune:
         from thunderrw_gb300 import autotune
-        if args.workload == "ppr":
-            res = autotune.tune(graph, E.PPR(wl["tp"]), src, walkers_per_query=per_q, rings=(1, 2), ctas=(0, 4),
-                                repeats=2)
+        if name == "ppr":
+            tr = autotune.tune(graph, app, src, walkers_per_query=per_q, rings=(1, 2), ctas=(0, 4), repeats=2)
         else:
-            res = autotune.tune(graph, app, src, rings=(1, 2, 4), ctas=(0, 2, 4), repeats=2)
-        shape = {"slot": res.sampler, "walkers_per_lane": res.best[0], "ctas_per_sm": res.best[1],
-                 "tuned_on_walkers": res.walkers, "candidates": len(res.timings)}
+            tr = autotune.tune(graph, app, src, rings=(1, 2, 4), ctas=(0, 2, 4), repeats=2)
+        shape = {"slot": tr.sampler, "walkers_per_lane": tr.best[0], "ctas_per_sm": tr.best[1],
+                 "tuned_on_walkers": tr.walkers, "candidates": len(tr.timings)}
         torch.cuda.synchronize()
+    res["engine"] = {"engine": "persistent", "launch_shape": shape,
+                     "output": ("sparse CSR per query (offsets, vertex, int32 count)" if sparse else
+                                "dense int32 [Q][N], zeroed every step" if name == "ppr" else
+                                "int32 paths [W][L] + lengths")}
 
     # ---- warm-up
-    for i in range(args.warmup):
+    for i in range(warmup):
         one_step(1000 + i)
     torch.cuda.synchronize()
 
     # ---- timed region: K whole batches, fresh seeds
-    sampler = ClockSampler(local)
-    sampler.start()
+    sampler = ClockSampler(dev.index or 0) if headline else None
+    if sampler:
+        sampler.start()
     if world > 1:
+        import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    total_steps = 0
-    # Working sets that fit in L2 (the 129 MB L2) are flushed between timed
-    # steps by writing a 512 MB buffer outside the events; larger inputs need
-    # no flush.
-    working = graph.e * 4 + graph.n * 8 + (graph.e * 16 if args.workload == "deepwalk" else 0)
-    flush_l2 = working < 2 * 129e6
+    flush_l2 = needs_l2_flush(name, graph.n, graph.e)
     flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device=dev) if flush_l2 else None
     if flush_l2:
         t_total = 0.0
-        for i in range(args.steps):
+        for i in range(steps):
             flush_buf.fill_(i & 0xFF)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -393,16 +503,18 @@ def run_ours(args):
     else:
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        for i in range(args.steps):
+        for i in range(steps):
             one_step(2000 + i)
         ev1.record(stream)
         torch.cuda.synchronize()
         t_total = ev0.elapsed_time(ev1) / 1e3
     # per-launch walk-kernel time: the library records CUDA events on the
-    # stream around its walk launch (and after the sparse post-processing)
+    # stream around its walk launch (and after the sparse post-processing);
+    # the same batches again, so the step counts are those of the timed ones
     graph.profile(True)
     kern_ms, post_ms = [], []
-    for i in range(args.steps):
+    total_steps = 0
+    for i in range(steps):
         if flush_l2:
             flush_buf.fill_(i & 0xFF)
         one_step(2000 + i)
@@ -411,10 +523,23 @@ def run_ours(args):
         post_ms.append(pms)
         total_steps += int(steps_dev.item())
     graph.profile(False)
-    clocks = sampler.stop()
-    steps_per_batch = total_steps / args.steps
-    t_total, all_steps = replicas.reduce_timing(t_total, steps_per_batch * args.steps, world, dev)
-    value = all_steps / t_total
+    if sampler:
+        res["clocks"] = sampler.stop()
+    steps_per_batch = total_steps / steps
+    t_total, all_steps = replicas.reduce_timing(t_total, steps_per_batch * steps, world, dev)
+    res.update(value=all_steps / t_total, ms_per_step=t_total / steps * 1e3, measured_steps_per_batch=steps_per_batch,
+               gpu_launches=launches_per_step * steps)
+
+    host = host_arrays(inp) if (rank == 0 and (not args.no_parity or not args.no_cpu)) else None
+    # ---- parity: the last batch above (seed 2000 + steps - 1) against the oracle, untimed
+    if not args.no_parity and outputs is not None and host is not None:
+        t0 = time.perf_counter()
+        ok, what = parity_sample(name, wl, host, replicas.replica_seed(2000 + steps - 1, rank), outputs,
+                                 inp.get("per_query", 0))
+        res["parity_checked"] = bool(ok)
+        res["parity"] = "%s (%.1f s, untimed)" % (what, time.perf_counter() - t0)
+    else:
+        res["parity_checked"] = False
 
     # ---- e2e: through the C ABI with host buffers (pinned sources in, results out)
     h_src = src.cpu().pin_memory()
@@ -423,89 +548,86 @@ def run_ours(args):
         h_off = torch.empty(Q + 1, dtype=torch.int64).pin_memory()
         h_vert = torch.empty(cap, dtype=torch.int32).pin_memory()
         h_vcnt = torch.empty(cap, dtype=torch.int32).pin_memory()
-    elif args.workload != "ppr":
+    elif name != "ppr":
         h_paths = torch.empty((W, wl["length"]), dtype=torch.int32).pin_memory()  # the walks' result
     torch.cuda.synchronize()
 
     def e2e_step(i):
-        if args.workload == "ppr" and sparse:
+        if sparse:
             d = E.PPR(wl["tp"]).desc(replicas.replica_seed(3000 + i, rank))
-            N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
-                                           ctypes.c_void_p(h_off.data_ptr()), ctypes.c_void_p(h_vert.data_ptr()),
-                                           ctypes.c_void_p(h_vcnt.data_ptr()), cap, ctypes.c_void_p(h_steps.data_ptr()),
-                                           0, ctypes.c_void_p(stream.cuda_stream)))
+            N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), _c(h_src), Q, per_q, _c(h_off),
+                                           _c(h_vert), _c(h_vcnt), cap, _c(h_steps), 0, sp))
             return int(h_steps.item()), 8 * (Q + 1) + 8 * int(h_off[-1].item()) + 8
-        elif args.workload == "ppr":
+        elif name == "ppr":
             d = E.PPR(wl["tp"]).desc(replicas.replica_seed(3000 + i, rank))
-            N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), Q, per_q,
-                                    ctypes.c_void_p(counts.data_ptr()), ctypes.c_void_p(h_steps.data_ptr()), 1, 0,
-                                    ctypes.c_void_p(stream.cuda_stream)))
+            N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), _c(h_src), Q, per_q, _c(counts), _c(h_steps),
+                                    1, 0, sp))
             return int(h_steps.item()), 8
         d = app.desc(replicas.replica_seed(3000 + i, rank))
-        N.check(L.trw_walk(graph.handle, ctypes.byref(d), ctypes.c_void_p(h_src.data_ptr()), W, 0,
-                           ctypes.c_void_p(h_paths.data_ptr()), wl["length"], None, None,
-                           ctypes.c_void_p(h_steps.data_ptr()), 0, ctypes.c_void_p(stream.cuda_stream)))
+        N.check(L.trw_walk(graph.handle, ctypes.byref(d), _c(h_src), W, 0, _c(h_paths), wl["length"], None, None,
+                           _c(h_steps), 0, sp))
         return int(h_steps.item()), h_paths.numel() * 4 + 8
 
     e2e_step(-1)  # untimed: the first host-buffer call allocates its staging and copy streams
     torch.cuda.synchronize()
+    e2e_n = steps if headline else min(steps, 3)
     t0 = time.perf_counter()
     e2e_steps, d2h = 0, 0
-    for i in range(args.steps):
+    for i in range(e2e_n):
         s_i, b_i = e2e_step(i)
         e2e_steps += s_i
         d2h += b_i
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
-    e2e = {"value": e2e_steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": int(h_src.numel() * 4),
-           "d2h_bytes_per_step": int(d2h / max(1, args.steps))}
+    res["e2e"] = {"value": e2e_steps / e2e_t, "unit": "steps/s", "h2d_bytes_per_step": int(h_src.numel() * 4),
+                  "d2h_bytes_per_step": int(d2h / max(1, e2e_n))}
 
-    # ---- plain one-launch-per-query form (the comparison engine)
-    plain = None
+    # ---- plain forms (the comparison engine: one thread per walker, no refill)
     if not args.no_plain:
-        reps = max(1, min(3, args.steps))
+        reps = max(1, min(3, steps))
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if args.workload == "ppr":
-            # one launch per query, one thread per walker, no refill
+        a.record(stream)
+        for r in range(reps):
+            one_step(4000 + r, engine="plain")
+        b.record(stream)
+        torch.cuda.synchronize()
+        t1 = a.elapsed_time(b) / 1e3 / reps
+        res["plain_one_launch"] = {"value": steps_per_batch / t1, "unit": "steps/s", "ms_per_step": t1 * 1e3,
+                                   "form": "one launch over the whole batch, one thread per walker, no refill"}
+        res["vs_plain_one_launch"] = res["value"] / res["plain_one_launch"]["value"]
+        if name == "ppr":
+            # one launch per query (the plain one-kernel-per-query form)
             a.record(stream)
             for r in range(reps):
                 for qi in range(Q):
                     d = E.PPR(wl["tp"]).desc(4000 + r)
                     qsrc = ctypes.c_void_p(src.data_ptr() + 4 * qi)
                     if sparse:
-                        N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), qsrc, 1, per_q,
-                                                       ctypes.c_void_p(offsets.data_ptr()),
-                                                       ctypes.c_void_p(vert.data_ptr()),
-                                                       ctypes.c_void_p(vcnt.data_ptr()), cap,
-                                                       ctypes.c_void_p(steps_dev.data_ptr()), 1,
-                                                       ctypes.c_void_p(stream.cuda_stream)))
+                        N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), qsrc, 1, per_q, _c(offsets),
+                                                       _c(vert), _c(vcnt), cap, _c(steps_dev), 1, sp))
                     else:
                         N.check(L.trw_ppr_batch(graph.handle, ctypes.byref(d), qsrc, 1, per_q,
                                                 ctypes.c_void_p(counts.data_ptr() + 4 * qi * graph.n),
-                                                ctypes.c_void_p(steps_dev.data_ptr()), 1, 1,
-                                                ctypes.c_void_p(stream.cuda_stream)))
+                                                _c(steps_dev), 1, 1, sp))
             b.record(stream)
             torch.cuda.synchronize()
+            t2 = a.elapsed_time(b) / 1e3 / reps
+            res["plain"] = {"value": steps_per_batch / t2, "unit": "steps/s", "ms_per_step": t2 * 1e3,
+                            "form": "one launch per query, one thread per walker, no refill"}
         else:
-            a.record(stream)
-            for r in range(reps):
-                one_step(4000 + r, engine="plain")
-            b.record(stream)
-            torch.cuda.synchronize()
-        plain_t = a.elapsed_time(b) / 1e3 / reps
-        plain = {"value": steps_per_batch / plain_t, "unit": "steps/s", "ms_per_step": plain_t * 1e3,
-                 "form": "one thread per walker, one launch per query, no refill"}
+            res["plain"] = res["plain_one_launch"]
+        res["vs_plain"] = res["value"] / res["plain"]["value"]
 
     # ---- roofline of the walk kernel
     kmean = statistics.mean(kern_ms) / 1e3
-    if args.workload in BYTES_PER_STEP:
-        bps = BYTES_PER_STEP[args.workload]
+    if name in BYTES_PER_STEP:
+        bps = BYTES_PER_STEP[name]
     else:
         # Algorithmic bytes per move of the timed walks (the last batch's
         # paths, first 65536 walkers) under the kernel's own access pattern.
         sample = paths[:65536].cpu().numpy()
-        if args.workload == "node2vec":
+        if name == "node2vec":
             bps = bytes_model.node2vec(sample, wl["length"])
         elif graph.indexes()[1] == 1:  # MetaPath answered from the label index
             bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"])
@@ -519,52 +641,62 @@ def run_ours(args):
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    # DRAM bytes per step from the committed ncu summary of the same kernel,
-    # scaled to this launch by its step count
-    import glob
-    import re
-    for md in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        key = "ppr_dense" if args.workload == "ppr" and not sparse else args.workload
-        m = re.search(r"traffic_bytes_per_step_%s = ([0-9.]+)" % key, open(md).read())
-        if m:
-            traffic = float(m.group(1)) * steps_per_batch
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "bytes_per_step": bps, "kernel_ms": kmean * 1e3,
-            "post_ms": statistics.mean(post_ms) if sparse else None,
-            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    tkey = "ppr_dense" if name == "ppr" and not sparse else name
+    traffic = TRAFFIC_BYTES_PER_STEP[tkey] * steps_per_batch if tkey in TRAFFIC_BYTES_PER_STEP else None
+    res["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "traffic": traffic, "bytes_per_step": bps, "kernel_ms": kmean * 1e3,
+                       "post_ms": statistics.mean(post_ms) if sparse else None,
+                       "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        row = inp["row"].cpu().numpy()
-        adj = inp["adj"].cpu().numpy()
-        wt = inp["weight"].cpu().numpy() if inp["weight"] is not None else None
-        lab = inp["label"].cpu().numpy() if inp.get("label") is not None else None
-        v, sample, cores = cpu_baseline(args.workload, wl, row, adj, wt, src.cpu().numpy(),
-                                        inp.get("per_query", 0), args.cpu_seconds, 0, label=lab)
-        cpu = {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
+    # ---- CPU baseline (rank 0 only)
+    if host is not None and not args.no_cpu:
+        cb = cpu_baseline(name, wl, host, inp.get("per_query", 0), args.cpu_seconds if headline else
+                          args.cpu_seconds / 3)
+        res["cpu_baseline"] = dict(cb, unit="steps/s", kind="port")
+    graph.close()
+    del inp, graph
+    torch.cuda.empty_cache()
+    return res
 
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    res = measure(args.workload, args, args, dev, rank, world, args.steps, args.warmup, headline=True)
+    side = {}
+    if not args.no_workloads and args.workload == "ppr" and not args.scale and not args.queries:
+        plain_args = SimpleNamespace(scale=None, queries=None)
+        for name in SIDE_WORKLOADS:
+            r = measure(name, args, plain_args, dev, rank, world, args.side_steps, max(3, args.warmup // 2),
+                        headline=False)
+            side[name] = {k: r[k] for k in ("config", "value", "ms_per_step", "e2e", "roofline", "plain",
+                                             "vs_plain", "parity_checked", "parity", "cpu_baseline", "engine")
+                          if k in r}
     if rank == 0:
         line = {
-            "metric": "walk_steps_per_s", "value": value, "unit": "steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3,
+            "metric": "walk_steps_per_s", "value": res["value"], "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
             "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": workload_name(wl, args), "n": graph.n, "e": graph.e,
-                       "steps_per_batch": steps_per_batch, "engine": "persistent",
-                       "launch_shape": shape or "automatic (0 = automatic)",
-                       "counts": ("dense int32 [Q][N], zeroed every step" if args.workload == "ppr" and not sparse
-                                  else "sparse CSR per query (offsets, vertex, int32 count)")
-                       if args.workload == "ppr" else None,
-                       "l2": ("L2 flushed between timed steps (512 MB write outside the events)" if flush_l2 else
-                              "inputs larger than L2 (adjacency %.2f GB, counts %.1f GB), no flush" % (
-                                  graph.e * 4 / 1e9, (counts.numel() * 4 / 1e9) if counts is not None else 0))},
+            "config": res["config"],
+            "engine": res["engine"],
+            "measured_steps_per_batch": res["measured_steps_per_batch"],
             "kernel_timing": "walk-kernel CUDA events recorded by the library on the launch stream",
-            "gpu_launches": args.steps, "clocks": clocks, "e2e": e2e, "roofline": roof,
-            "plain": plain, "vs_plain": (value / plain["value"]) if plain else None, "cpu_baseline": cpu,
+            "gpu_launches": res["gpu_launches"], "clocks": res.get("clocks"), "e2e": res["e2e"],
+            "roofline": res["roofline"], "plain": res.get("plain"), "vs_plain": res.get("vs_plain"),
+            "plain_one_launch": res.get("plain_one_launch"), "vs_plain_one_launch": res.get("vs_plain_one_launch"),
+            "parity_checked": res["parity_checked"], "parity": res.get("parity"),
+            "cpu_baseline": res.get("cpu_baseline"),
         }
+        if side:
+            line["workloads"] = side
         print(json.dumps(line), flush=True)
-    graph.close()
     if world > 1:
         dist.destroy_process_group()
     return 0
@@ -576,7 +708,6 @@ def run_serving(args):
     MetaPath, walkers log-uniform in [1e3, 1e6], lengths uniform in [5, 80].
     Reports p50 / p99 latency (submit -> results complete in HBM) and steps/s
     per arrival rate."""
-    import threading
     import torch
     from thunderrw_gb300 import engine as E
     from thunderrw_gb300 import generators as G

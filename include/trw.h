@@ -240,7 +240,8 @@ int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_p
  * before any stream capture.  All calls on a device share the array: the
  * call clears the work-queue head and step counter it keeps there, and
  * calls that overlap on the GPU race on it, so serialise them (one stream,
- * or events). */
+ * or events).  The call holds the graph's lock from its checks through the
+ * launch, like trw_walk, and is timed by trw_profile_read like any walk. */
 int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources,
                                    int64_t num_walkers, int64_t id_base, int32_t *paths, int32_t path_cap,
                                    int32_t *lengths, int32_t *counts, uint64_t *steps, trw_stream_t stream);

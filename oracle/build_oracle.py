@@ -60,7 +60,18 @@ def ref_tool_cmds(reference_root):
              "-o", os.path.join(out_dir, "edgelist_to_csr"), "-pthread"]]
 
 
-def build(reference_root="/root/reference", with_ref=True):
+# Where this recipe reads the reference tree: the TRW_REFERENCE_ROOT
+# environment variable, else the read-only mount of the build container.
+# Machines without the tree (the GPU hosts) build the oracle alone.
+REFERENCE_MOUNT = "/root/reference"
+
+
+def reference_root_default():
+    return os.environ.get("TRW_REFERENCE_ROOT") or REFERENCE_MOUNT
+
+
+def build(reference_root=None, with_ref=True):
+    reference_root = reference_root or reference_root_default()
     cmds = [oracle_cmd()]
     if with_ref and os.path.isdir(os.path.join(reference_root, "random_walk")):
         cmds += ref_cmds(reference_root) + ref_tool_cmds(reference_root)

@@ -65,7 +65,9 @@ def cases():
     return out
 
 
-def main(reference_root="/root/reference"):
+def main(reference_root=None):
+    """reference_root: the reference tree (default: build_oracle's
+    TRW_REFERENCE_ROOT / mount rule)."""
     build_oracle.build(reference_root, with_ref=True)
     graphs, arrays, manifest = {}, {}, {"philox_kat": PHILOX_KAT, "graphs": GRAPHS, "cases": []}
     gobjs = {}

@@ -32,7 +32,7 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-@pytest.mark.parametrize("app_name", ["deepwalk", "node2vec", "metapath"])
+@pytest.mark.parametrize("app_name", ["deepwalk", "node2vec", "metapath", "ppr", "genericwalk"])
 def test_noalloc_matches_trw_walk_on_two_calls(app_name):
     from tests.gpu_util import need_gpu
     torch, E = need_gpu()
@@ -43,9 +43,17 @@ def test_noalloc_matches_trw_walk_on_two_calls(app_name):
     graph = E.Graph(g["row"], g["adj"], g["weight"], g["label"])
     try:
         L = 25
+        # trw_walk runs dynamic-mode PPR and GenericWalk on the static alias
+        # tables (walker-independent weights); this entry point always runs
+        # the per-step dynamic kernel, so these two cases also check that
+        # both forms give the same walks
         app = {"deepwalk": E.DeepWalk(L, mode="dynamic", sampler="alias"),
                "node2vec": E.Node2Vec(L, 2.0, 0.5, sampler="alias"),
-               "metapath": E.MetaPath(L, [0, 1, 2, 3, 4], sampler="alias")}[app_name]
+               "metapath": E.MetaPath(L, [0, 1, 2, 3, 4], sampler="alias"),
+               "ppr": E.PPR(0.25, mode="dynamic", sampler="alias"),
+               "genericwalk": E.GenericWalk(L, mode="dynamic", sampler="alias")}[app_name]
+        if app_name == "ppr":
+            app.path_cap = L
         src = G.all_sources(g["row"], seed=3)[:3000].cuda()
         W = src.numel()
         ref = E.compute(graph, src, app, seed=5, id_base=11, count_visits=True)
@@ -129,5 +137,63 @@ def test_noalloc_node2vec_before_edge_set():
         torch.cuda.synchronize()
         assert torch.equal(paths, ref.paths) and torch.equal(lengths, ref.lengths)
         assert int(steps.item()) == ref.steps
+    finally:
+        graph.close()
+
+
+def test_noalloc_is_profiled_and_holds_the_graph_lock():
+    """With profiling on, trw_profile_read reports this entry point's own walk
+    (not an earlier trw_walk's), and calls from several host threads on one
+    stream give the walks of serial calls (the entry point takes the graph's
+    lock while another thread's trw_walk builds the edge set)."""
+    import threading
+
+    from tests.gpu_util import need_gpu
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+
+    g = G.make_graph("rmat", 1 << 12, 12, seed=79)
+    graph = E.Graph(g["row"], g["adj"], g["weight"])
+    try:
+        L = 30
+        app = E.Node2Vec(L, 2.0, 0.5, sampler="alias")
+        src = G.all_sources(g["row"], seed=5)[:2500].cuda()
+        W = src.numel()
+        f = _entry(N)
+        stream = torch.cuda.current_stream()
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        # a short trw_walk first, so a stale reading would show its duration
+        E.compute(graph, src[:64], E.DeepWalk(3, mode="dynamic", sampler="its"), seed=1)
+        torch.cuda.synchronize()
+        graph.profile(True)
+        E.compute(graph, src[:64], E.DeepWalk(3, mode="dynamic", sampler="its"), seed=1)
+        short_ms, _ = graph.last_timings()
+        paths = torch.full((W, L), -7, dtype=torch.int32, device="cuda")
+        lengths = torch.full((W,), -7, dtype=torch.int32, device="cuda")
+        d = app.desc(8)
+        N.check(f(graph.handle, ctypes.byref(d), _ptr(src), W, 0, _ptr(paths), L, _ptr(lengths), None, None, sp))
+        walk_ms, post_ms = graph.last_timings()
+        graph.profile(False)
+        assert walk_ms > 0.0 and post_ms == 0.0
+        assert walk_ms != short_ms
+        # one thread builds the edge set through trw_walk while another calls the entry point
+        out = {}
+
+        def via_trw_walk():
+            with torch.cuda.stream(stream):
+                out["ref"] = E.compute(graph, src, app, seed=9)
+
+        paths2 = torch.full((W, L), -7, dtype=torch.int32, device="cuda")
+        lengths2 = torch.full((W,), -7, dtype=torch.int32, device="cuda")
+        t = threading.Thread(target=via_trw_walk)
+        t.start()
+        d9 = app.desc(9)
+        rc = f(graph.handle, ctypes.byref(d9), _ptr(src), W, 0, _ptr(paths2), L, _ptr(lengths2), None, None, sp)
+        t.join()
+        assert rc == 0, N.load().trw_last_error()
+        torch.cuda.synchronize()
+        assert torch.equal(paths2, out["ref"].paths) and torch.equal(lengths2, out["ref"].lengths)
+        assert graph.device_error() == 0
     finally:
         graph.close()

@@ -1193,6 +1193,11 @@ extern "C" int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc 
     for (const void *q : ptrs)
         if (q && !is_device_ptr(q))
             return fail(TRW_ERR_INVALID, "the no-alloc entry point takes device pointers only (staging would allocate)");
+    // The graph's lookup structures (edge set, label index), launch shapes
+    // and profiling events are written by other calls under this lock; hold
+    // it from the plan through the launch, as trw_walk does.  A lock
+    // allocates nothing.
+    std::lock_guard<std::mutex> lock(g->mu);
     Plan pl;
     int rc = make_plan(g, desc, pl);
     if (rc) return rc;
@@ -1233,8 +1238,13 @@ extern "C" int trw_walk_dynamic_alias_noalloc(trw_graph *g, const trw_walk_desc 
     shape.engine = kEnginePersistent;
     shape.num_sms = g->num_sms;
     shape.max_warps = std::min(warps, warp_engine_warps(p, shape));
+    if (g->profile) {  // event records allocate nothing
+        TRW_CUDA(cudaEventRecord(g->ev_walk0, st));
+        g->have_post = false;
+    }
     const cudaError_t le = launch_walk_warp(p, kAlias, pl.update, pl.weight_kind, shape, st);
     if (le != cudaSuccess) return fail(TRW_ERR_CUDA, "walk launch: %s", cudaGetErrorString(le));
+    if (g->profile) TRW_CUDA(cudaEventRecord(g->ev_walk1, st));
     if (steps) TRW_CUDA(cudaMemcpyAsync(steps, state + 1, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
     return TRW_OK;
 }
