@@ -423,8 +423,8 @@ def measure(name, args, over, dev, rank, world, steps, warmup, headline):
                 d = E.PPR(wl["tp"]).desc(replicas.replica_seed(seed, rank))
                 N.check(L.trw_ppr_batch_sparse(graph.handle, ctypes.byref(d), _c(src), Q, per_q, _c(offsets),
                                                _c(vert), _c(vcnt), cap, _c(steps_dev), N.ENGINES[engine], sp))
-            # the walk and the post-processing kernel (one query range)
-            launches_per_step = 2
+            # walk, distinct, segment scan, offsets scan, emit (one query range)
+            launches_per_step = 5
         else:
             counts = torch.empty((Q, graph.n), dtype=torch.int32, device=dev)
             outputs = None

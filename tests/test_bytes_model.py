@@ -69,3 +69,23 @@ def test_constant_models(graph):
     d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=6)
     nb, ns = O.count_bytes(graph, d, src, per_query=20, record_paths=False, count_visits=True)
     assert nb / ns == B.UNIFORM_PPR
+
+
+def test_sector_reuse_counts_hot_sectors():
+    """Walks that all leave one source through its one neighbour: the
+    source's row-pair sector and the neighbour's adjacency sector take a
+    large share of the reads, and an L2-sized cache holds every sector."""
+    from thunderrw_gb300 import bytes_model as B
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("rmat", 1 << 12, 8, seed=3, weights=False)
+    row, adj = g["row"].numpy(), g["adj"].numpy()
+    og = O.Graph(row, adj)
+    src = np.full(64, int(np.argmax(np.diff(row))), dtype=np.int32)
+    r = O.walk(og, O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=3), src, per_query=100,
+               path_cap=32)
+    out = B.sector_reuse(r["paths"], row, adj, cache_bytes=(1024, 129 << 20))
+    assert out["moves"] > 0
+    assert out["row_pair_hit_132096KB"] == 1.0 and out["adjacency_hit_132096KB"] == 1.0
+    assert 0.0 < out["row_pair_hit_1KB"] <= 1.0
+    share = B.top_degree_share(r["paths"], row, ks=(1, 4096))
+    assert share[4096] == 1.0 and share[1] > 0.0  # every walk starts at the highest-degree vertex

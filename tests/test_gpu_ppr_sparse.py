@@ -233,31 +233,3 @@ def test_sparse_host_weighted_ranges(rmat):
             np.testing.assert_array_equal(dense, ref["counts"][0])
     finally:
         g.close()
-
-
-def test_sparse_log_segments_overflow():
-    """In the persistent engine's log form every move goes to its item's
-    segment for the vertex's sub-table, and moves beyond a segment's room go
-    to the query's overflow region.  On a two-vertex graph every move of an
-    item lands in one segment and some items (64 walkers, 320 moves expected)
-    exceed its 384 entries: the counts must still be the oracle's, the order
-    the table form's (plain engine), and no error is raised."""
-    torch, E = need_gpu()
-    row = np.array([0, 1, 2], dtype=np.int64)
-    adj = np.array([1, 0], dtype=np.int32)
-    qs = np.array([0, 1, 0, 1, 1, 0, 0, 1], dtype=np.int32)
-    ref = O.walk(O.Graph(row, adj), O.make_desc("ppr", "uniform", "uniform", length=1, tp=0.2, seed=41), qs,
-                 per_query=20_000, want_counts=True, want_lengths=False)
-    g = E.Graph(row, adj)
-    try:
-        a = E.ppr_batch_sparse(g, qs, 20_000, tp=0.2, seed=41, engine="persistent")
-        b = E.ppr_batch_sparse(g, qs, 20_000, tp=0.2, seed=41, engine="plain")
-        assert a.steps == ref["steps"]
-        _check_against_dense(a, ref["counts"])
-        total = int(a.offsets[-1].item())
-        assert torch.equal(a.offsets, b.offsets)
-        assert torch.equal(a.vertices[:total], b.vertices[:total])
-        assert torch.equal(a.counts[:total], b.counts[:total])
-        assert g.device_error() == 0
-    finally:
-        g.close()

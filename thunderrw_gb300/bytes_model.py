@@ -94,3 +94,49 @@ def metapath_index(paths: np.ndarray, row: np.ndarray, length: int) -> float:
         return 0.0
     last = _stops(p, length)
     return (frm.size * (SECTOR * 2 + 4) + SECTOR * last.size) / frm.size
+
+
+def sector_reuse(paths: np.ndarray, row: np.ndarray, adj: np.ndarray, cache_bytes=(227 << 10, 129 << 20)):
+    """How much an ideal cache of the hottest 32-byte sectors could serve of
+    the walks' random reads: for each cache size, the fraction of row-pair
+    reads and of adjacency reads that fall in the most-read sectors of the
+    whole sample (chosen with hindsight, so an upper bound for any staging of
+    rows in shared memory or L2).  A move from u to v reads u's row pair
+    (8-byte pairs) and the adjacency entry holding v in u's sorted row."""
+    frm, to, _, _ = _moves(paths)
+    row = np.asarray(row, dtype=np.int64)
+    adj = np.asarray(adj)
+    out = {"moves": int(frm.size)}
+    if frm.size == 0:
+        return out
+    # position of `to` in frm's sorted row, searched row by row
+    order = np.argsort(frm, kind="stable")
+    f, t = frm[order], to[order]
+    pos = np.empty(f.size, dtype=np.int64)
+    starts = np.flatnonzero(np.r_[True, f[1:] != f[:-1]])
+    ends = np.r_[starts[1:], f.size]
+    for a, b in zip(starts, ends):
+        u = f[a]
+        lo, hi = row[u], row[u + 1]
+        pos[a:b] = lo + np.searchsorted(adj[lo:hi], t[a:b])
+    for name, sec in (("row_pair", f * 8 // SECTOR), ("adjacency", pos * 4 // SECTOR)):
+        _, cnt = np.unique(sec, return_counts=True)
+        cnt = np.sort(cnt)[::-1]
+        cum = np.cumsum(cnt)
+        out[name + "_distinct_sectors"] = int(cnt.size)
+        for cb in cache_bytes:
+            k = min(cnt.size, cb // SECTOR)
+            out["%s_hit_%dKB" % (name, cb >> 10)] = float(cum[k - 1] / cum[-1]) if k > 0 else 0.0
+    return out
+
+
+def top_degree_share(paths: np.ndarray, row: np.ndarray, ks=(1024, 4096, 8192, 65536)):
+    """Fraction of the moves that start at one of the k highest-degree
+    vertices (their row pairs are what a shared-memory table of hub rows
+    keyed by vertex could serve), for each k."""
+    frm, _, _, _ = _moves(paths)
+    deg = np.diff(np.asarray(row, dtype=np.int64))
+    rank = np.empty(deg.size, dtype=np.int64)
+    rank[np.argsort(-deg, kind="stable")] = np.arange(deg.size)
+    r = rank[frm]
+    return {int(k): float((r < k).mean()) if frm.size else 0.0 for k in ks}

@@ -136,12 +136,12 @@ struct trw_graph {
     DevBuf alias_scratch;
     cudaEvent_t scratch_done = nullptr;
     LaunchShape shape[5];
-    // sparse PPR: per-query visit tables of the table form (kept all-zero
-    // between batches) and output staging
+    // sparse PPR: per-query visit tables (kept all-zero between batches),
+    // per-query distinct-vertex counts and output staging
     DevBuf ppr_tables;
     int32_t ppr_bits = 0;
     int64_t ppr_queries = 0;
-    bool ppr_dirty = false;  // a table-form batch stopped between its walk and its post-processing
+    bool ppr_dirty = false;  // a batch stopped between its walk and its emit
     cudaEvent_t ppr_done = nullptr;  // last sparse batch's emit: the tables are free after it
     cudaEvent_t tables_done = nullptr;  // last static-table build: walks on any stream wait for it
     // optional per-call timing: events around the walk launch and after the
@@ -149,8 +149,7 @@ struct trw_graph {
     bool profile = false;
     cudaEvent_t ev_walk0 = nullptr, ev_walk1 = nullptr, ev_post1 = nullptr;
     bool have_post = false;
-    DevBuf ppr_meta;  // look-back words, tile counters, step counts, log fill counts, overflow regions
-    DevBuf ppr_log;   // log form: one log per item of kLogItem walkers
+    DevBuf ppr_distinct;
     DevBuf stage_out;
     // sparse PPR into host buffers: a second compute stream and a copy
     // stream, per-range events (offsets scanned, range finished) and pinned
@@ -473,20 +472,12 @@ int ensure_host_pipeline(trw_graph *g) {
     return TRW_OK;
 }
 
-// Visit logs of one range of a sparse PPR batch (log form).
-struct LogArgs {
-    int32_t *log, *fill, *ovf, *ovf_n;
-    int32_t seg;      // entries per item segment
-    int32_t ovf_cap;  // overflow entries per query
-    int64_t items_per_query;
-};
-
 // Shared implementation of trw_walk and trw_ppr_batch.
 int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
              int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
              int32_t *lengths, int32_t *counts, int64_t counts_len, bool zero_counts, uint64_t *steps,
              int32_t engine, cudaStream_t st, int32_t *table = nullptr, int32_t table_bits = 0,
-             bool hold_lock = false, const LogArgs *log = nullptr) {
+             bool hold_lock = false) {
     if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
     if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
     if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
@@ -597,15 +588,6 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     p.error = g->error;
     p.table = table;
     p.table_bits = table_bits;
-    if (log) {
-        p.log = log->log;
-        p.log_fill = log->fill;
-        p.log_ovf = log->ovf;
-        p.log_ovf_n = log->ovf_n;
-        p.log_seg = log->seg;
-        p.log_ovf_cap = log->ovf_cap;
-        p.items_per_query = log->items_per_query;
-    }
 
     LaunchShape shape = g->shape[pl.sampler == kLabelIndex ? (int)kITS : pl.sampler];
     shape.engine = engine;
@@ -619,7 +601,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
         // when there are too few walkers to give every lane several; four
         // otherwise.
         const int64_t lanes = (int64_t)g->num_sms * 2048;
-        shape.ring = (table || log || pl.sampler == kMaxRejection || num_walkers < 4 * lanes) ? 1 : 4;
+        shape.ring = (table || pl.sampler == kMaxRejection || num_walkers < 4 * lanes) ? 1 : 4;
     }
     cudaError_t le;
     if (g->profile) {
@@ -935,70 +917,24 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     TRW_CUDA(cudaStreamWaitEvent(st, g->ppr_done, 0));
     // Table size: 2^bits >= 1.25 x the expected visits of a query (walkers /
     // tp), which bounds its distinct vertices, and never above 2 x the vertex
-    // count (a query cannot visit more).  The table is cut into sub-tables of
-    // 2^sb slots, one post-processing tile each.
+    // count (a query cannot visit more).
     const double visits = (double)walkers_per_query / desc->tp;
     int32_t bits = 10;
     while (bits < 30 && (double)(1ll << bits) < 1.25 * visits) ++bits;
     while (bits > 10 && (1ll << (bits - 1)) >= 2ll * g->n) --bits;
-    const int32_t pbits = bits - sub_bits(bits);
-    // Log form on the persistent engine: every move appends its vertex to its
-    // item's log (kLogItem walkers of one query), in the segment of the
-    // vertex's sub-table, and each post-processing tile reads its own
-    // segments.  Visits are not spread evenly over the sub-tables (all of an
-    // item's walkers first move to the few neighbours of their source), so a
-    // segment holds an item's expected moves plus 64; what does not fit goes
-    // to the query's overflow region (a quarter of its expected visits, at
-    // least 4096 entries).  Only the entries written are ever touched.  For
-    // queries of at most kLogMaxSegs sub-tables and kLogMaxItems items;
-    // otherwise the walk inserts into per-query tables in global memory
-    // (table form).
-    const int64_t ipq = (walkers_per_query + kLogItem - 1) / kLogItem;
-    const double seg_d = (double)kLogItem / desc->tp + 64.0;
-    const int32_t log_seg = seg_d < (double)(1 << 20) ? (((int32_t)seg_d + 3) & ~3) : 0;
-    const double ovf_d = std::max(4096.0, visits / 4.0);
-    const int32_t ovf_cap = ovf_d < (double)(1 << 24) ? (((int32_t)ovf_d + 3) & ~3) : 0;
-    const int64_t items = num_queries * ipq;
-    const size_t log_bytes = sizeof(int32_t) * (size_t)items * ((size_t)log_seg << pbits);
-    bool use_log = engine == TRW_ENGINE_PERSISTENT && (1 << pbits) <= kLogMaxSegs && log_seg > 0 && ovf_cap > 0 &&
-                   ipq <= kLogMaxItems && ((items << pbits) < (1ll << 31)) && num_queries > 0;
-    if (use_log) {
-        size_t free_b = 0, total_b = 0;
-        TRW_CUDA(cudaMemGetInfo(&free_b, &total_b));
-        if (log_bytes > g->ppr_log.bytes && log_bytes > free_b / 4) use_log = false;
+    if (num_queries > 0 && (g->ppr_bits != bits || g->ppr_queries < num_queries || g->ppr_dirty)) {
+        const size_t bytes = sizeof(int2) * ((size_t)num_queries << bits);
+        TRW_CUDA(g->ppr_tables.ensure(bytes));
+        TRW_CUDA(cudaMemsetAsync(g->ppr_tables.p, 0, bytes, st));
+        g->ppr_bits = bits;
+        g->ppr_queries = num_queries;
     }
-    int32_t *tables = nullptr, *log = nullptr;
-    if (use_log) {
-        TRW_CUDA(g->ppr_log.ensure(log_bytes));
-        log = static_cast<int32_t *>(g->ppr_log.p);
-    } else if (num_queries > 0) {
-        if (g->ppr_bits != bits || g->ppr_queries < num_queries || g->ppr_dirty) {
-            const size_t bytes = sizeof(int2) * ((size_t)num_queries << bits);
-            TRW_CUDA(g->ppr_tables.ensure(bytes));
-            TRW_CUDA(cudaMemsetAsync(g->ppr_tables.p, 0, bytes, st));
-            g->ppr_bits = bits;
-            g->ppr_queries = num_queries;
-        }
-        tables = static_cast<int32_t *>(g->ppr_tables.p);
-    }
-    // per-call state: look-back words and tile counters (zeroed), log fill
-    // counts and overflow counts (zeroed), step counts, overflow regions
-    const int64_t nq1 = std::max<int64_t>(1, num_queries);
-    const size_t b_status = align_up(sizeof(unsigned long long) * (size_t)(nq1 << pbits));
-    const size_t b_tiles = align_up(sizeof(unsigned int) * kMaxRanges);
-    const size_t b_fill = use_log ? align_up(sizeof(int32_t) * ((size_t)items << pbits)) : 0;
-    const size_t b_ovfn = use_log ? align_up(sizeof(int32_t) * (size_t)nq1) : 0;
-    const size_t b_steps = align_up(sizeof(uint64_t) * (kMaxRanges + 1));
-    const size_t b_ovf = use_log ? align_up(sizeof(int32_t) * (size_t)nq1 * (size_t)ovf_cap) : 0;
-    TRW_CUDA(g->ppr_meta.ensure(b_status + b_tiles + b_fill + b_ovfn + b_steps + b_ovf));
-    char *mb = static_cast<char *>(g->ppr_meta.p);
-    unsigned long long *status = reinterpret_cast<unsigned long long *>(mb);
-    unsigned int *tile_next = reinterpret_cast<unsigned int *>(mb + b_status);
-    int32_t *log_fill = reinterpret_cast<int32_t *>(mb + b_status + b_tiles);
-    int32_t *ovf_n = reinterpret_cast<int32_t *>(mb + b_status + b_tiles + b_fill);
-    uint64_t *d_steps = reinterpret_cast<uint64_t *>(mb + b_status + b_tiles + b_fill + b_ovfn);
-    int32_t *ovf = reinterpret_cast<int32_t *>(mb + b_status + b_tiles + b_fill + b_ovfn + b_steps);
-    TRW_CUDA(cudaMemsetAsync(mb, 0, b_status + b_tiles + b_fill + b_ovfn, st));
+    const int64_t dist_ints = ppr_distinct_ints(bits);  // per query: total + segment prefixes
+    const size_t b_dist = align_up(sizeof(int32_t) * (size_t)dist_ints * (size_t)std::max<int64_t>(1, num_queries));
+    TRW_CUDA(g->ppr_distinct.ensure(b_dist + sizeof(uint64_t) * (kMaxRanges + 1)));
+    int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
+    int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
+    uint64_t *d_steps = reinterpret_cast<uint64_t *>(static_cast<char *>(g->ppr_distinct.p) + b_dist);
 
     // staging for host buffers: sources in; offsets, vertices, counts out
     const bool h_src = num_queries > 0 && !is_device_ptr(sources);
@@ -1031,8 +967,7 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     // produced, so it hides behind the next walk).  Ranges
     // alternate between two compute streams so that the next range's walk
     // fills the GPU while the last walkers of a range finish; only the
-    // post-processing kernels are chained across ranges (each range's first
-    // tile starts from the previous range's last offset).  Every range keeps at least 8
+    // offsets scans are chained across ranges.  Every range keeps at least 8
     // walkers per lane of the GPU.  bounds[r] .. bounds[r + 1] = range r.
     std::vector<int64_t> bounds{0};
     if (host_out && num_queries > 1) {
@@ -1069,53 +1004,26 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         TRW_CUDA(cudaStreamWaitEvent(rs[1], g->ev_fork, 0));
     }
     int nr = 0;
-    if (tables) g->ppr_dirty = true;
+    g->ppr_dirty = true;
     for (; nr < ranges; ++nr) {
         const int64_t qs = bounds[nr], nq = bounds[nr + 1] - qs;
         const cudaStream_t sr = rs[nr & 1];
-        int32_t *tab = tables ? tables + (qs << (bits + 1)) : nullptr;
-        LogArgs la{};
-        if (log) {
-            la.log = log + ((qs * ipq) << pbits) * (int64_t)log_seg;
-            la.fill = log_fill + ((qs * ipq) << pbits);
-            la.ovf = ovf + qs * (int64_t)ovf_cap;
-            la.ovf_n = ovf_n + qs;
-            la.seg = log_seg;
-            la.ovf_cap = ovf_cap;
-            la.items_per_query = ipq;
-        }
+        int32_t *tab = tables + (qs << (bits + 1));
+        int32_t *dist = distinct + dist_ints * qs;
         int rc = run_walk(g, desc, d_src + qs, nq, nq * walkers_per_query, walkers_per_query, qs * walkers_per_query,
                           nullptr, 0, nullptr, nullptr, 0, false, d_steps + nr, engine, sr, tab, bits,
-                          /*hold_lock=*/true, log ? &la : nullptr);
+                          /*hold_lock=*/true);
         if (rc) {
             // earlier ranges are still queued on both streams: let them finish before returning
             if (rs[1] != st) cudaStreamSynchronize(rs[1]);
             cudaStreamSynchronize(st);
             return rc;
         }
-        // the range's first tile reads offsets[qs], written by the previous range's post-processing
         if (nr > 0 && rs[1] != st) TRW_CUDA(cudaStreamWaitEvent(sr, g->offsets_done[nr - 1], 0));
-        PprPost pp{};
-        pp.tables = tab;
-        pp.log = la.log;
-        pp.log_fill = la.fill;
-        pp.log_ovf = la.ovf;
-        pp.log_ovf_n = la.ovf_n;
-        pp.log_seg = log_seg;
-        pp.log_ovf_cap = ovf_cap;
-        pp.items_per_query = (int32_t)ipq;
-        pp.bits = bits;
-        pp.nq = nq;
-        pp.offsets = d_off + qs;
-        pp.status = status + (qs << pbits);
-        pp.tile_next = tile_next + nr;
-        pp.vout = d_v;
-        pp.cout = d_c;
-        pp.capacity = capacity;
-        pp.error = g->error;
-        TRW_CUDA(launch_ppr_post(pp, sr));
+        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, sr));
+        if (host_out) TRW_CUDA(cudaEventRecord(g->offsets_done[nr], sr));
+        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, sr));
         if (host_out) {
-            TRW_CUDA(cudaEventRecord(g->offsets_done[nr], sr));
             TRW_CUDA(cudaMemcpyAsync(g->h_ends + nr, d_off + qs + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, sr));
             TRW_CUDA(cudaEventRecord(g->range_done[nr], sr));
         }
@@ -1161,10 +1069,10 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         if (err) {
             TRW_CUDA(cudaMemset(g->error, 0, sizeof(int)));
             if (err & kErrCapacity)
-                return fail(TRW_ERR_CAPACITY, "sparse PPR output needs %lld entries, capacity is %lld (or a "
-                            "visit table / log overflow region ran full)", (long long)total, (long long)capacity);
-            return fail(TRW_ERR_DEVICE, "device error word %d (1 = rejection trial limit, 2 = invalid source vertex, "
-                        "8 = post-processing look-back wait ran out)", err);
+                return fail(TRW_ERR_CAPACITY, "sparse PPR output needs %lld entries, capacity is %lld",
+                            (long long)total, (long long)capacity);
+            return fail(TRW_ERR_DEVICE, "device error word %d (1 = rejection trial limit, 2 = invalid source vertex)",
+                        err);
         }
     }
     return TRW_OK;

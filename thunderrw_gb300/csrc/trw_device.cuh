@@ -147,9 +147,7 @@ enum WeightKind : int { kEdgeWeight = 0, kUnitWeight = 1, kNode2Vec = 2, kLabelS
 constexpr int kMaxSchema = 64;
 constexpr uint32_t kMaxTrials = 1u << 20;
 
-// device error word bits: rejection trial limit, invalid source, a sparse
-// table or output without room, a look-back wait that ran out
-enum DeviceError : int { kErrTrials = 1, kErrVertex = 2, kErrCapacity = 4, kErrLookback = 8 };
+enum DeviceError : int { kErrTrials = 1, kErrVertex = 2, kErrCapacity = 4 };
 
 struct WalkParams {
     DevGraph g;
@@ -182,72 +180,37 @@ struct WalkParams {
     // dynamic alias scratch: one table of max_degree slots per warp
     AliasSlot *alias_scratch;
     int64_t alias_scratch_stride;
-    // sparse visit counts, table form: per query an open-addressing table of
-    // 2^table_bits slots stored as 2^table_bits keys (vertex + 1, 0 = empty)
-    // followed by 2^table_bits counts (visits minus one).  Keys and counts
-    // live in separate sectors so that reading a hot key never queues behind
-    // the atomic adds to its count.
+    // sparse visit counts: per query an open-addressing table of 2^table_bits
+    // slots stored as 2^table_bits keys (vertex + 1, 0 = empty) followed by
+    // 2^table_bits counts (visits minus one).  Keys and counts live in
+    // separate sectors so that reading a hot key never queues behind the
+    // atomic adds to its count.
     int32_t *table;
     int32_t table_bits;
-    // sparse visit counts, log form: walker batches are cut into items of
-    // kLogItem consecutive walkers of one query; every move appends its
-    // vertex to its item's log, in the segment of the vertex's sub-table
-    // (2^(table_bits - sub_bits) segments of log_seg entries per item, then
-    // the query's overflow region of log_ovf_cap entries)
-    int32_t *log;
-    int32_t *log_fill;   // per item and segment: entries in it (written when the item closes)
-    int32_t *log_ovf;    // per query: overflow entries
-    int32_t *log_ovf_n;  // per query: overflow entries written (beyond log_ovf_cap: error)
-    int32_t log_seg;
-    int32_t log_ovf_cap;
-    int64_t items_per_query;
 };
 
-// Sparse visit tables are split into sub-tables of at most 2^kSubBits slots,
-// each small enough for one CTA's shared memory: a vertex's home slot is
-// hash(v) >> (32 - bits) as usual, its sub-table the home slot's top bits,
-// and linear probing wraps around inside the sub-table.  Which slots of a
-// sub-table end up occupied, and which keys each run of occupied slots
-// holds, do not depend on the order of the inserts.
-constexpr int32_t kSubBits = 13;
-constexpr int32_t kLogItem = 64;        // walkers per log item
-constexpr int32_t kLogMaxSegs = 8;      // log form: at most 8 sub-tables per query
-constexpr int32_t kLogMaxItems = 2048;  // log form: at most 2048 items per query
-
-__host__ __device__ __forceinline__ int32_t sub_bits(int32_t bits) { return bits < kSubBits ? bits : kSubBits; }
-
-__device__ __forceinline__ uint32_t ppr_home(int32_t v, int32_t bits) {
-    return ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
-}
-
-// The slot after h in h's sub-table of 2^sb slots.
-__device__ __forceinline__ uint32_t ppr_next(uint32_t h, int32_t sb) {
-    const uint32_t m = (1u << sb) - 1u;
-    return (h & ~m) | ((h + 1u) & m);
-}
-
 // Adds `inc` visits of vertex v to a query's table t (keys t[0..C), counts
-// t[C..2C)): linear probing on key v + 1, 0 = empty, inside v's sub-table.
-// A slot's count holds its visits minus one: the CAS that claims the slot
-// stands for the first.
+// t[C..2C)): linear probing on key v + 1, 0 = empty.  A slot's count holds
+// its visits minus one: the CAS that claims the slot stands for the first.
+// Which slots end up occupied does not depend on the insertion order; only
+// the order of keys inside a run of occupied slots does.
 __device__ __forceinline__ void table_add(int32_t *t, int32_t bits, int32_t v, int inc, int *error) {
-    const int32_t sb = sub_bits(bits);
-    const uint32_t C = 1u << bits;
-    uint32_t h = ppr_home(v, bits);
+    const uint32_t mask = (1u << bits) - 1u;
+    uint32_t h = ((uint32_t)v * 0x9E3779B1u) >> (32 - bits);
     const int32_t key = v + 1;
-    for (uint32_t probe = 0; probe < (1u << sb); ++probe) {
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
         int k = __ldcg(t + h);
         if (k == 0) {
             k = atomicCAS(t + h, 0, key);
             if (k == 0) {  // claimed
-                if (inc > 1) atomicAdd(t + C + h, inc - 1);
+                if (inc > 1) atomicAdd(t + mask + 1 + h, inc - 1);
                 return;
             }
         }
-        if (k == key) { atomicAdd(t + C + h, inc); return; }
-        h = ppr_next(h, sb);
+        if (k == key) { atomicAdd(t + mask + 1 + h, inc); return; }
+        h = (h + 1) & mask;
     }
-    atomicOr(error, kErrCapacity);  // sub-table full: every slot holds another vertex
+    atomicOr(error, kErrCapacity);  // table full: every slot holds another vertex
 }
 
 // Records a move to `v` for walker query q (dense counts or the sparse

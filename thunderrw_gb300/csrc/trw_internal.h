@@ -28,28 +28,15 @@ cudaError_t launch_walk_warp(const WalkParams &p, int sampler, int update, int w
 // number of per-warp dynamic-alias scratch tables the warp engine will use
 int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
 
-// Sparse PPR post-processing of nq queries (one range of a batch): builds
-// each (query, sub-table) tile's counts in shared memory from the visit logs
-// (log != nullptr) or from the walk's tables (which it zeroes), and writes
-// the CSR entries and offsets[1..nq]; offsets[0] must hold the entries
-// before this range (0 for the first).  status (nq << (bits - sub_bits(bits))
-// words) and *tile_next must be zero.
-struct PprPost {
-    int32_t *tables;
-    const int32_t *log, *log_fill, *log_ovf, *log_ovf_n;
-    int32_t log_seg, log_ovf_cap;
-    int32_t items_per_query;
-    int32_t bits;
-    int64_t nq;
-    int64_t *offsets;
-    unsigned long long *status;
-    unsigned int *tile_next;
-    int32_t *vout, *cout;
-    int64_t capacity;
-    int *error;
-};
-cudaError_t launch_ppr_post(const PprPost &pp, cudaStream_t st);
-size_t ppr_post_smem(int32_t bits);
+// offsets[0] must hold the entries before this range of queries (0 for the first)
+cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
+                               cudaStream_t st);
+// `distinct` holds nq totals followed by ppr_distinct_ints(bits) - 1 segment
+// prefixes per query (ppr_distinct_ints(bits) ints per query in all)
+int64_t ppr_distinct_ints(int32_t bits);
+cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
+                            const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
+                            cudaStream_t st);
 // *out = parts[0] + ... + parts[n-1], on the device
 cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st);
 

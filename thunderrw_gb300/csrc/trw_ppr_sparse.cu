@@ -1,37 +1,34 @@
-// trw_ppr_sparse.cu -- sparse per-query PPR visit counts: the post-processing
-// kernel that turns a batch's visits into CSR (offsets, vertex, count).
+// trw_ppr_sparse.cu -- sparse per-query PPR visit counts.
 //
-// Each query's counts live in an open-addressing table of 2^bits slots (key
-// vertex + 1, 0 = empty), cut into sub-tables of 2^sb slots, sb =
-// sub_bits(bits) <= 13; a vertex's sub-table is the top bits of its home slot
-// and linear probing wraps around inside the sub-table (trw_device.cuh).  A
-// sub-table fits one CTA's shared memory (64 KB at sb = 13, three CTAs per
-// SM), so one CTA handles one (query, sub-table) tile:
-//  * build the sub-table in shared memory, either from the query's visit
-//    logs (the persistent engine's log form: the walk appended every move to
-//    its item's segment for the vertex's sub-table, so the tile reads only its
-//    own segments) or from the table the walk filled in global memory (table
-//    form: plain engine, very large queries), which it then zeroes;
-//  * count its occupied slots and find the tile's output offset by a
-//    decoupled look-back over the tiles before it (tiles are claimed in
-//    order from a counter, so every tile it waits for is running);
-//  * write its entries: the runs of occupied slots in slot order with the
-//    keys of each run sorted, the run that wraps around the sub-table's end
-//    last.  Which slots are occupied and which keys each run holds do not
-//    depend on the order of the inserts, so the output is a function of the
-//    counts (and the table geometry) alone.
-// Tiles go in (query, sub-table) order, so a query's entries are contiguous.
+// During the walk every move adds the new vertex to its query's
+// open-addressing table (table_add, trw_device.cuh).  Walker ids are claimed
+// in increasing order, so only the tables of the few dozen queries whose
+// walkers are in flight are being written at any time and they stay in L2;
+// the dense query-major alternative (4 x N bytes per query) would need its
+// whole count array zeroed every batch.
+//
+// After the walk:
+//  * distinct_kernel + segment_scan_kernel + offsets_kernel: occupied slots
+//    per warp segment of each table, their prefix within the query, then the
+//    queries' totals scanned into CSR offsets (offsets[q] .. offsets[q+1] hold query
+//    q's entries), continuing from offsets[0] so that a batch can run as
+//    several ranges of queries;
+//  * emit_kernel (one CTA per chunk of at most 2^16 slots): writes the
+//    (vertex, count) pairs.  With
+//    linear probing the SET of occupied slots does not depend on the order of
+//    insertion, only the order of keys inside each run of occupied slots
+//    does; so the kernel emits runs in slot order (the run that wraps around
+//    the table end last) with the keys inside each run sorted, which makes
+//    the output a function of the visit counts alone.  It then zeroes the
+//    table for the next batch.
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
 namespace trw {
 namespace {
 
-constexpr int kPostThreads = 512;  // three CTAs (tiles) per SM at sb = 13
-constexpr unsigned long long kFlagAgg = 1ull << 62;   // tile count published
-constexpr unsigned long long kFlagPref = 1ull << 63;  // tile's inclusive offset published
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr uint32_t kLookbackSpins = 1u << 17;  // per window of predecessors, ~100 ns each
+constexpr int kScanThreads = 1024;
+constexpr int kEmitThreads = 512;
 
 template <typename T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T &total) {
@@ -61,221 +58,208 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T &total) {
     return excl;
 }
 
-// Adds one visit of v (if `mine`) to the shared-memory sub-table; lanes with
-// the same vertex are merged first (a query's walkers revisit the vertices
-// around its source).
-__device__ __forceinline__ void smem_add(int32_t *keys, int32_t *cnts, uint32_t M, uint32_t home, int32_t v,
-                                         bool mine, int *error) {
-    if (!mine) return;
-    const unsigned peers = __match_any_sync(__activemask(), v);
-    if ((int)(threadIdx.x & 31) != __ffs(peers) - 1) return;
-    const int inc = __popc(peers);
-    const int32_t key = v + 1;
-    volatile int32_t *vk = keys;
-    uint32_t h = home & (M - 1u);
-    for (uint32_t probe = 0; probe < M; ++probe) {
-        int32_t k = vk[h];
-        if (k == 0) k = atomicCAS(keys + h, 0, key);
-        if (k == 0 || k == key) {
-            atomicAdd(cnts + h, inc);
-            return;
-        }
-        h = (h + 1u) & (M - 1u);
-    }
-    atomicOr(error, kErrCapacity);  // the sub-table is full
+constexpr int kEmitWarps = kEmitThreads / 32;  // table segments per CTA
+constexpr int32_t kChunkBits = 16;             // at most 2^16 slots per CTA
+
+// A table of 2^bits slots is split into chunks_for(bits) chunks of at most
+// 2^16 slots, one CTA each, and every chunk into kEmitWarps warp segments;
+// a single large table (a query with many walkers) is then spread over the
+// GPU instead of one CTA.
+__host__ __device__ inline uint32_t chunks_for(int32_t bits) {
+    return bits > kChunkBits ? 1u << (bits - kChunkBits) : 1u;
 }
 
-__global__ void __launch_bounds__(kPostThreads, 3) ppr_post_kernel(const PprPost pp) {
-    extern __shared__ __align__(16) int32_t sm[];
-    __shared__ long long s_tile, s_excl;
-    __shared__ uint32_t s_head, s_tail;
-    __shared__ int32_t s_sums[32];
-    const int32_t sb = sub_bits(pp.bits);
-    const uint32_t M = 1u << sb, W = M >> 5;  // bits >= 10: W >= 32 words
-    const int32_t pbits = pp.bits - sb;        // sub-tables per query: 2^pbits
-    int32_t *keys = sm, *cnts = sm + M;
-    uint32_t *words = reinterpret_cast<uint32_t *>(sm + 2 * M);
-    int32_t *wpre = reinterpret_cast<int32_t *>(words + W);
-    int32_t *ipre = wpre + W;  // log form: prefix of the query's item segment lengths
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-
-    if (tid == 0) s_tile = (long long)atomicAdd(pp.tile_next, 1u);
-    int4 *sm4 = reinterpret_cast<int4 *>(sm);
-    for (uint32_t i = tid; i < M / 2; i += blockDim.x) sm4[i] = make_int4(0, 0, 0, 0);
-    __syncthreads();
-    const int64_t tile = s_tile;
-    const int64_t q = tile >> pbits;
-    const uint32_t sub = (uint32_t)(tile & ((1ll << pbits) - 1));
-
-    // ---- build the sub-table
-    if (pp.tables) {
-        // the walk's global table: counts hold visits minus one; zero it for the next batch
-        int4 *tk = reinterpret_cast<int4 *>(pp.tables + (q << (pp.bits + 1)) + ((int64_t)sub << sb));
-        int4 *tc = reinterpret_cast<int4 *>(pp.tables + (q << (pp.bits + 1)) + (1ll << pp.bits) + ((int64_t)sub << sb));
-        int4 *k4 = sm4, *c4 = reinterpret_cast<int4 *>(cnts);
-        for (uint32_t i = tid; i < M / 4; i += blockDim.x) {
-            const int4 k = __ldcg(tk + i), c = __ldcg(tc + i);
-            k4[i] = k;
-            c4[i] = make_int4(k.x ? c.x + 1 : 0, k.y ? c.y + 1 : 0, k.z ? c.z + 1 : 0, k.w ? c.w + 1 : 0);
-            tk[i] = make_int4(0, 0, 0, 0);
-            tc[i] = make_int4(0, 0, 0, 0);
-        }
-    } else {
-        // This tile's segment of each of the query's item logs: a prefix over
-        // their lengths in shared memory, then one flattened loop in which
-        // every thread loads four entries before inserting them.
-        const int32_t ipq = pp.items_per_query;  // <= kLogMaxItems
-        const int64_t seg0 = (q * ipq << pbits) + sub;  // segment of the query's first item
-        int32_t carry = 0;
-        for (int32_t b = 0; b < ipq; b += blockDim.x) {
-            const int32_t i = b + tid;
-            const int32_t n = i < ipq ? __ldcg(pp.log_fill + seg0 + ((int64_t)i << pbits)) : 0;
-            int32_t tot;
-            const int32_t ex = block_exclusive_scan<int32_t>(n, s_sums, tot);
-            if (i < ipq) ipre[i] = carry + ex;
-            carry += tot;
-        }
-        if (tid == 0) ipre[ipq] = carry;
-        __syncthreads();
-        const int32_t entries = carry;
-        for (int32_t e0 = 0; e0 < entries; e0 += 4 * (int32_t)blockDim.x) {
-            int32_t v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int32_t e = e0 + u * (int32_t)blockDim.x + tid;
-                v[u] = -1;
-                if (e < entries) {
-                    int32_t lo = 0, hi = ipq;  // item i with ipre[i] <= e < ipre[i + 1]
-                    while (hi - lo > 1) {
-                        const int32_t mid = (lo + hi) >> 1;
-                        if (ipre[mid] <= e) lo = mid; else hi = mid;
-                    }
-                    v[u] = __ldcg(pp.log + (seg0 + ((int64_t)lo << pbits)) * pp.log_seg + (e - ipre[lo]));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t home = v[u] >= 0 ? ppr_home(v[u], pp.bits) : 0u;
-                smem_add(keys, cnts, M, home, v[u], v[u] >= 0, pp.error);
-            }
-        }
-        // the query's overflow entries (rare), those of this sub-table
-        const int32_t no = min(__ldcg(pp.log_ovf_n + q), pp.log_ovf_cap);
-        for (int32_t j = tid; j < no; j += blockDim.x) {
-            const int32_t v = __ldcg(pp.log_ovf + q * pp.log_ovf_cap + j);
-            const uint32_t home = ppr_home(v, pp.bits);
-            smem_add(keys, cnts, M, home, v, (home >> sb) == sub, pp.error);
-        }
+// Occupied slots (distinct visited vertices) per warp segment: seg[(q * S +
+// chunk) * kEmitWarps + warp].
+__global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *tables, int32_t bits, int32_t *seg) {
+    const uint32_t S = chunks_for(bits);
+    const int64_t q = blockIdx.x / S;
+    const uint32_t c = blockIdx.x % S;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t chunk = (1u << bits) / S;
+    const uint32_t seg4 = chunk / kEmitWarps / 4;  // int4 per segment
+    const int4 *keys = reinterpret_cast<const int4 *>(tables + (q << (bits + 1)) + (size_t)c * chunk) + warp * seg4;
+    uint32_t n = 0;
+    for (uint32_t i = lane; i < seg4; i += 32) {
+        const int4 k = __ldg(keys + i);
+        n += (k.x != 0) + (k.y != 0) + (k.z != 0) + (k.w != 0);
     }
-    __syncthreads();
+#pragma unroll
+    for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (lane == 0) seg[((int64_t)blockIdx.x) * kEmitWarps + warp] = (int32_t)n;
+}
 
-    // ---- occupancy words, their prefix counts and the wrap-around run
-    for (uint32_t w = warp; w < W; w += nwarps) {
-        const unsigned b = __ballot_sync(0xffffffffu, keys[w * 32 + lane] != 0);
-        if (lane == 0) words[w] = b;
+// Per query: the segment counts become their exclusive prefix within the
+// query (in place) and the query's total goes to distinct[q].
+__global__ void __launch_bounds__(kScanThreads) segment_scan_kernel(int32_t *seg, int32_t bits, int32_t *distinct) {
+    __shared__ int32_t sums[32];
+    const int64_t q = blockIdx.x;
+    const int32_t n = (int32_t)chunks_for(bits) * kEmitWarps;
+    int32_t *v = seg + q * n;
+    int32_t carry = 0;
+    for (int32_t b = 0; b < n; b += kScanThreads) {
+        const int32_t i = b + threadIdx.x;
+        const int32_t x = i < n ? v[i] : 0;
+        int32_t total;
+        const int32_t ex = block_exclusive_scan<int32_t>(x, sums, total);
+        if (i < n) v[i] = carry + ex;
+        carry += total;
     }
-    __syncthreads();
-    int32_t total;
-    const int32_t pc = tid < (int)W ? __popc(words[tid]) : 0;  // W <= 256 < blockDim
-    const int32_t pex = block_exclusive_scan<int32_t>(pc, s_sums, total);
-    if (tid < (int)W) wpre[tid] = pex;
-    if (tid == 0) {
+    if (threadIdx.x == 0) distinct[q] = carry;
+}
+
+// offsets[0] holds the entries of the queries before this range (0 for the
+// first range of a batch); offsets[1..nq] become the running totals.
+__global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *distinct, int64_t nq, int64_t *offsets) {
+    __shared__ int64_t sums[32];
+    int64_t carry = offsets[0];  // read by every thread before the first write below
+    for (int64_t b = 0; b < nq; b += kScanThreads) {
+        const int64_t i = b + threadIdx.x;
+        const int64_t v = i < nq ? (int64_t)distinct[i] : 0;
+        int64_t total;
+        const int64_t ex = block_exclusive_scan<int64_t>(v, sums, total);
+        if (i < nq) offsets[i] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) offsets[nq] = carry;
+}
+
+// One CTA per chunk of at most 2^16 slots of a query's table, one contiguous
+// segment of the chunk per warp.
+//
+// Output order.  Inserts probe linearly and wrap from the last slot to slot
+// 0, so the occupied slots form maximal runs on a cycle; which slots are
+// occupied, and which keys each run holds, do not depend on the order of the
+// inserts, only the order of the keys inside a run does.  The entries are
+// written run by run in slot order, each run's keys sorted, except that the
+// run wrapping around the table end (if any) comes last.  Each occupied slot
+// finds its own output position:
+//   pos = (occupied slots before it) - (slots of the wrapping run at the table
+//         start) - (its distance back to the run start) + (rank of its key
+//         among the run's keys)
+// A warp walks its segment 32 slots at a time with coalesced loads and keeps
+// the previous, current and next blocks of keys in registers (two more blocks
+// in flight): the run of a slot is found from the three occupancy ballots and
+// its key ranked against the run through shuffles.  Runs reaching beyond that
+// 96-slot window, and the wrapping run, are read from global memory, which
+// stays intact until the final zeroing.
+__global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, const int64_t *offsets,
+                                                            const int32_t *seg_prefix, int32_t *vout, int32_t *cout,
+                                                            int64_t capacity, int *error) {
+    __shared__ uint32_t wrap[2];
+    const uint32_t S = chunks_for(bits);
+    const int64_t q = blockIdx.x / S;
+    const uint32_t chunk = blockIdx.x % S;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nslots = 1u << bits;
+    int32_t *keys = tables + (q << (bits + 1));
+    int32_t *cnts = keys + nslots;
+    const int64_t end = offsets[q + 1];
+    const bool write = end <= capacity;
+    if (threadIdx.x == 0) {
+        if (!write && chunk == 0) atomicOr(error, kErrCapacity);
+        // the wrapping run: `head` slots from slot 0 and `tail` slots before the end
         uint32_t head = 0, tail = 0;
-        if ((words[0] & 1u) && (words[W - 1] >> 31) && total < (int32_t)M) {
-            for (uint32_t w = 0;; ++w) {
-                const uint32_t inv = ~words[w];
-                if (inv) { head += __ffs(inv) - 1; break; }
-                head += 32;
-            }
-            for (uint32_t w = W - 1;; --w) {
-                const uint32_t inv = ~words[w];
-                if (inv) { tail += __clz(inv); break; }
-                tail += 32;
+        if (__ldg(keys) != 0 && __ldg(keys + nslots - 1) != 0) {
+            while (head < nslots && __ldg(keys + head) != 0) ++head;
+            if (head < nslots) {
+                while (__ldg(keys + nslots - 1 - tail) != 0) ++tail;
+            } else {
+                head = 0;  // a full table (the walk reported it) has no run boundary
             }
         }
-        s_head = head;
-        s_tail = tail;
-    }
-
-    // ---- the tile's output offset: decoupled look-back by warp 0, over 32
-    // predecessors per round trip (lane i examines tile j - i)
-    if (warp == 0) {
-        int64_t excl = 0;
-        if (tile == 0) {
-            excl = pp.offsets[0];
-        } else {
-            if (lane == 0) atomicExch(pp.status + tile, kFlagAgg | (unsigned long long)total);
-            int64_t j = tile - 1;
-            uint32_t spins = 0;
-            for (;;) {
-                const int64_t idx = j - lane;
-                // before the first tile: a neutral prefix of 0 (tile 0 always publishes one)
-                const unsigned long long w = idx >= 0 ? *reinterpret_cast<volatile unsigned long long *>(pp.status + idx)
-                                                      : (unsigned long long)kFlagPref;
-                const unsigned pref = __ballot_sync(0xffffffffu, (w & kFlagPref) != 0);
-                const unsigned any = __ballot_sync(0xffffffffu, (w & (kFlagPref | kFlagAgg)) != 0);
-                int take = -1;  // lanes 0..take are summed
-                if (pref) {
-                    const int f = __ffs(pref) - 1;  // the nearest inclusive prefix
-                    const unsigned nearer = (1u << f) - 1u;
-                    if ((any & nearer) == nearer) take = f;
-                } else if (any == 0xffffffffu) {
-                    take = 31;
-                }
-                if (take >= 0) {
-                    unsigned long long v = lane <= take ? (w & kValMask) : 0ull;
-#pragma unroll
-                    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    excl += (int64_t)v;
-                    if (pref) break;
-                    j -= 32;
-                    spins = 0;
-                    continue;
-                }
-                if (++spins > kLookbackSpins) {  // a nearer tile has not published (cannot happen)
-                    if (lane == 0) atomicOr(pp.error, kErrLookback);
-                    break;
-                }
-                __nanosleep(100);
-            }
-        }
-        if (lane == 0) {
-            atomicExch(pp.status + tile, kFlagPref | (unsigned long long)(excl + total));
-            s_excl = excl;
-            if (sub == 0) pp.offsets[q] = excl;
-            if (tile == (pp.nq << pbits) - 1) pp.offsets[pp.nq] = excl + total;
-            if (excl + total > pp.capacity) atomicOr(pp.error, kErrCapacity);
-        }
+        wrap[0] = head;
+        wrap[1] = tail;
     }
     __syncthreads();
+    const uint32_t head = wrap[0], tail = wrap[1], cyc = head + tail;
+    int64_t prefix = offsets[q] + seg_prefix[(int64_t)blockIdx.x * kEmitWarps + warp];
 
-    // ---- entries in canonical order
-    const int64_t excl = s_excl;
-    if (excl + total > pp.capacity) return;
-    const uint32_t head = s_head, tail = s_tail, cyc = head + tail;
-    for (uint32_t x = tid; x < M; x += blockDim.x) {
-        const int32_t k = keys[x];
-        if (k == 0) continue;
-        int32_t pos;
-        if (x < head || x + tail >= M) {  // the wrap-around run: last, keys sorted
-            uint32_t rank = 0;
-            for (uint32_t i = 0; i < cyc; ++i) {
-                const uint32_t y = i < tail ? M - tail + i : i - tail;
-                rank += keys[y] < k;
-            }
-            pos = total - (int32_t)cyc + (int32_t)rank;
-        } else {
-            uint32_t back = 0;
-            while (x > back && keys[x - back - 1] != 0) ++back;
-            uint32_t rank = 0;
-            for (uint32_t d = 1; d <= back; ++d) rank += keys[x - d] < k;
-            for (uint32_t y = x + 1; y < M && keys[y] != 0; ++y) rank += keys[y] < k;
-            const uint32_t before = (uint32_t)wpre[x >> 5] + __popc(words[x >> 5] & ((1u << (x & 31)) - 1u));
-            pos = (int32_t)(before - head - back + rank);
+    const uint32_t seg = nslots / S / kEmitWarps;  // >= 64: tables have >= 1024 slots, chunks 2^16
+    const uint32_t lo = chunk * (nslots / S) + warp * seg, nblk = seg / 32;
+    const uint32_t x0 = lo + lane;
+    auto key_at = [&](uint32_t y) { return y < nslots ? __ldg(keys + y) : 0; };
+    auto cnt_at = [&](uint32_t y) { return y < nslots ? __ldg(cnts + y) : 0; };
+    int32_t kp = lo ? __ldg(keys + lo - 32 + lane) : 0;
+    int32_t kc = key_at(x0), cc = cnt_at(x0);
+    int32_t kn = key_at(x0 + 32), cn = cnt_at(x0 + 32);
+    int32_t k2 = key_at(x0 + 64), c2 = cnt_at(x0 + 64);
+    unsigned op = __ballot_sync(0xffffffffu, kp != 0);
+    const unsigned lt = lanemask_lt(), le = lt | (1u << lane);
+    for (uint32_t b = 0; b < nblk; ++b) {
+        const uint32_t x = x0 + b * 32;
+        const int32_t k3 = key_at(x + 96), c3 = cnt_at(x + 96);
+        const unsigned oc = __ballot_sync(0xffffffffu, kc != 0), on = __ballot_sync(0xffffffffu, kn != 0);
+        const int64_t before = prefix + __popc(oc & lt);
+        prefix += __popc(oc);
+        const bool in_wrap = kc != 0 && (x < head || x >= nslots - tail);
+        // window positions: 0-31 previous block, 32-63 this block, 64-95 next block
+        int s = -1, e = -1;
+        if (kc != 0 && !in_wrap) {
+            const unsigned zb = ~oc & lt, za = ~oc & ~le;
+            if (zb) s = 64 - __clz(zb);
+            else if (~op) s = 32 - __clz(~op);
+            if (za) e = 31 + __ffs(za);
+            else if (~on) e = 63 + __ffs(~on);
         }
-        pp.vout[excl + pos] = k - 1;
-        pp.cout[excl + pos] = cnts[x];
+        const bool fast = s >= 0 && e >= 0;
+        const int len = fast ? e - s : 0;
+        const int maxlen = __reduce_max_sync(0xffffffffu, len);
+        uint32_t rank = 0;
+        if (__all_sync(0xffffffffu, !fast || (s >= 32 && e <= 64))) {
+            // every run of this block lies inside it: rank within this block's keys
+            for (int d = 0; d < maxlen; ++d) {
+                const int j = s + d;
+                const int32_t k = __shfl_sync(0xffffffffu, kc, j & 31);
+                if (d < len && j != 32 + lane) rank += k < kc;
+            }
+        } else {
+            for (int d = 0; d < maxlen; ++d) {
+                const int j = s + d;
+                const int src = j & 31;
+                const int32_t a = __shfl_sync(0xffffffffu, kp, src);
+                const int32_t m = __shfl_sync(0xffffffffu, kc, src);
+                const int32_t n = __shfl_sync(0xffffffffu, kn, src);
+                const int32_t k = j < 32 ? a : j < 64 ? m : n;
+                if (d < len && j != 32 + lane) rank += k < kc;
+            }
+        }
+        if (write && kc != 0) {
+            int64_t pos;
+            if (fast) {
+                pos = before - head - (32 + lane - s) + rank;
+            } else if (in_wrap) {
+                rank = 0;
+                for (uint32_t i = 0; i < cyc; ++i) {
+                    const uint32_t y = i < tail ? nslots - tail + i : i - tail;
+                    rank += __ldg(keys + y) < kc;
+                }
+                pos = end - cyc + rank;
+            } else {
+                uint32_t back = 0;
+                while (x > back && __ldg(keys + x - back - 1) != 0) ++back;
+                rank = 0;
+                for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + x - d) < kc;
+                for (uint32_t y = x + 1; y < nslots; ++y) {
+                    const int32_t k = __ldg(keys + y);
+                    if (k == 0) break;
+                    rank += k < kc;
+                }
+                pos = before - head - back + rank;
+            }
+            vout[pos] = kc - 1;
+            cout[pos] = cc + 1;  // the table counts visits after the first
+        }
+        kp = kc; op = oc;
+        kc = kn; cc = cn;
+        kn = k2; cn = c2;
+        k2 = k3; c2 = c3;
     }
+    if (S > 1) return;  // chunked tables are zeroed after the kernel: other CTAs may still read this chunk
+    __syncthreads();
+    // zero the table for the next batch (coalesced 16-byte stores)
+    int4 *z = reinterpret_cast<int4 *>(keys);
+    for (uint32_t i = threadIdx.x; i < nslots / 2; i += blockDim.x) z[i] = make_int4(0, 0, 0, 0);
 }
 
 __global__ void sum_steps_kernel(const unsigned long long *parts, int n, unsigned long long *out) {
@@ -292,18 +276,27 @@ cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaSt
     return cudaGetLastError();
 }
 
-size_t ppr_post_smem(int32_t bits) {
-    const size_t M = (size_t)1 << sub_bits(bits);
-    return 2 * M * sizeof(int32_t) + 2 * (M / 32) * sizeof(int32_t) + (kLogMaxItems + 1) * sizeof(int32_t);
+int64_t ppr_distinct_ints(int32_t bits) { return 1 + (int64_t)chunks_for(bits) * kEmitWarps; }
+
+cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
+                               cudaStream_t st) {
+    if (nq > 0) {
+        const int64_t ctas = nq * chunks_for(bits);
+        distinct_kernel<<<(unsigned)ctas, kEmitThreads, 0, st>>>(tables, bits, distinct + nq);
+        segment_scan_kernel<<<(unsigned)nq, kScanThreads, 0, st>>>(distinct + nq, bits, distinct);
+    }
+    offsets_kernel<<<1, kScanThreads, 0, st>>>(distinct, nq, offsets);
+    return cudaGetLastError();
 }
 
-cudaError_t launch_ppr_post(const PprPost &pp, cudaStream_t st) {
-    if (pp.nq <= 0) return cudaSuccess;
-    static const cudaError_t attr = cudaFuncSetAttribute(ppr_post_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)ppr_post_smem(30));
-    if (attr != cudaSuccess) return attr;
-    const int64_t tiles = pp.nq << (pp.bits - sub_bits(pp.bits));
-    ppr_post_kernel<<<(unsigned)tiles, kPostThreads, ppr_post_smem(pp.bits), st>>>(pp);
+cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
+                            const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
+                            cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    const uint32_t S = chunks_for(bits);
+    emit_kernel<<<(unsigned)(nq * S), kEmitThreads, 0, st>>>(tables, bits, offsets, distinct + nq, vout, cout,
+                                                             capacity, error);
+    if (S > 1) return cudaMemsetAsync(tables, 0, sizeof(int32_t) * 2 * ((size_t)nq << bits), st);
     return cudaGetLastError();
 }
 

@@ -67,7 +67,7 @@ __device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
     return s;
 }
 
-// A sparse visit-count insert in flight (kRecTable kernels), advanced once per
+// A sparse visit-count insert in flight (kSparse kernels), advanced once per
 // ring round so that no round trip stalls the warp:
 //  * recording a visit (end of round i) issues an L2 load of the key in the
 //    vertex's home slot;
@@ -111,41 +111,40 @@ __device__ __forceinline__ int32_t *table_of(const WalkParams &p, int32_t q) {
 // Advances the insert by one stage; with `blocking` it runs to completion.
 __device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, bool blocking) {
     if (pi.q < 0) return;
-    const int32_t sb = sub_bits(p.table_bits);
-    const uint32_t C = 1u << p.table_bits;
+    const uint32_t mask = (1u << p.table_bits) - 1u;
     int32_t *t = table_of(p, pi.q);
     const int32_t inc = (int32_t)(pi.meta & kIncMask);
     for (;;) {
         if (pi.meta & kCasBit) {
             if (pi.old == 0) { pi.q = -1; return; }  // claimed: its first visit is implied
             if (pi.old == pi.key) {                  // another warp claimed it for this vertex
-                atomicAdd(t + C + pi.h, 1);
+                atomicAdd(t + mask + 1 + pi.h, 1);
                 pi.q = -1;
                 return;
             }
-            if (inc > 1) atomicAdd(t + C + pi.h, 1 - inc);  // lost it to another vertex
+            if (inc > 1) atomicAdd(t + mask + 1 + pi.h, 1 - inc);  // lost it to another vertex
         } else {
             if (pi.old == pi.key) {
-                atomicAdd(t + C + pi.h, inc);
+                atomicAdd(t + mask + 1 + pi.h, inc);
                 pi.q = -1;
                 return;
             }
             if (pi.old == 0) {
                 pi.old = atomicCAS(t + pi.h, 0, pi.key);
-                if (inc > 1) atomicAdd(t + C + pi.h, inc - 1);  // speculative
+                if (inc > 1) atomicAdd(t + mask + 1 + pi.h, inc - 1);  // speculative
                 pi.meta |= kCasBit;
                 if (!blocking) return;
                 continue;
             }
         }
         const uint32_t probes = pi.meta >> 7;
-        if (probes >= kProbeLimit || probes + 1 >= (1u << sb)) {  // every slot of the sub-table holds another vertex
+        if (probes >= kProbeLimit || probes >= mask) {  // every slot holds another vertex
             atomicOr(p.error, kErrCapacity);
             pi.q = -1;
             return;
         }
         pi.meta = (pi.meta & kIncMask) + ((probes + 1) << 7);  // cas bit cleared
-        pi.h = ppr_next(pi.h, sb);
+        pi.h = (pi.h + 1) & mask;
         pi.old = __ldcg(t + pi.h);
         if (!blocking) return;
     }
@@ -154,86 +153,17 @@ __device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, 
 __device__ __forceinline__ void start_insert(const WalkParams &p, PendingInsert &pi, int32_t q, int32_t v, int inc) {
     if (pi.q >= 0) resolve(p, pi, true);  // filled a visit ago: normally already settled
     pi.q = q;
-    pi.h = ppr_home(v, p.table_bits);
+    pi.h = ((uint32_t)v * 0x9E3779B1u) >> (32 - p.table_bits);
     pi.key = v + 1;
     pi.meta = (uint32_t)inc;
     pi.old = __ldcg(table_of(p, pi.q) + pi.h);
 }
 
-// Where a kernel records visits: dense counts (or nowhere), the sparse
-// per-query tables (pipelined inserts), or the per-item visit logs.
-enum Recording : int { kRecCounts = 0, kRecTable = 1, kRecLog = 2 };
-
-// Log form of the sparse PPR counts.  A batch's walkers are cut into items of
-// kLogItem consecutive walkers of one query; the persistent engine claims
-// whole items, so all walkers of an item run on one warp, and the warp keeps
-// the item's fill counts in shared memory: appending a move costs one shared
-// atomic per group of lanes on the same item and segment and one 4-byte
-// store, and no global atomic.  An item closes when its last walker finishes
-// (its fill counts go to log_fill); the post-processing kernel then counts
-// each query's visits from its items' logs.
-struct LogItem {
-    int32_t item;                // -1 = free
-    int32_t live;                // walkers of the item running on this warp
-    int32_t admitted;            // 1 once every walker of the item has been admitted
-    int32_t fill[kLogMaxSegs];   // moves appended per sub-table segment (beyond log_seg: overflow region)
-};
-constexpr int kLogRing = 32;  // items a warp keeps open at once (one per lane for initialisation)
-
-struct LogCtx {
-    volatile LogItem *ring;  // this warp's items (shared memory)
-    int32_t slot;            // ring slot of this lane's walker's item
-};
-
-__device__ __forceinline__ void log_close(const WalkParams &p, volatile LogItem &it) {
-    const int32_t segs = 1 << (p.table_bits - sub_bits(p.table_bits));
-    for (int32_t k = 0; k < segs; ++k) p.log_fill[(int64_t)it.item * segs + k] = min((int32_t)it.fill[k], p.log_seg);
-    it.item = -1;
-}
-
-// Appends move `v` of this lane's walker to its item's log, in the segment
-// of v's sub-table (lanes on the same item and segment share one
-// shared-memory atomic).
-__device__ __forceinline__ void log_visit(const WalkParams &p, const LogCtx &lc, int32_t v) {
-    const int32_t sb = sub_bits(p.table_bits);
-    const uint32_t seg = ppr_home(v, p.table_bits) >> sb;
-    const unsigned peers = __match_any_sync(__activemask(), (uint32_t)lc.slot * kLogMaxSegs + seg);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd((int *)&lc.ring[lc.slot].fill[seg], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    const int pos = base + __popc(peers & lanemask_lt());
-    const int32_t item = lc.ring[lc.slot].item;
-    if (pos < p.log_seg) {
-        p.log[(((int64_t)item << (p.table_bits - sb)) + seg) * p.log_seg + pos] = v;
-    } else {  // a long item: the query's overflow region
-        const int32_t q = item / (int32_t)p.items_per_query;
-        const int o = atomicAdd(p.log_ovf_n + q, 1);
-        if (o < p.log_ovf_cap) p.log_ovf[(int64_t)q * p.log_ovf_cap + o] = v;
-        else atomicOr(p.error, kErrCapacity);
-    }
-}
-
-// This lane's walker has finished: the last one of an admitted item closes it.
-__device__ __forceinline__ void log_release(const WalkParams &p, const LogCtx &lc) {
-    const unsigned peers = __match_any_sync(__activemask(), lc.slot);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
-        volatile LogItem &it = lc.ring[lc.slot];
-        const int n = __popc(peers);
-        __threadfence_block();  // this group's appends before its release
-        if (atomicSub((int *)&it.live, n) == n) {
-            __threadfence_block();
-            if (it.admitted) log_close(p, it);
-        }
-    }
-}
-
-// One step for each of the R slots, stage by stage.  Rec says where visits
-// go (kRecTable: the pipelined inserts in `pend`; kRecLog: the item logs of
-// `lc`, ring depth 1 only).
-template <int S, int U, int WK, int R, int Rec>
+// One step for each of the R slots, stage by stage.  kSparse: visits go to
+// the per-query tables through the pipelined inserts in `pend`.
+template <int S, int U, int WK, int R, bool kSparse>
 __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uint64_t &steps,
-                                          PendingInsert (&pend)[R][kInsertDepth], const LogCtx &lc) {
+                                          PendingInsert (&pend)[R][kInsertDepth]) {
     const DevGraph &g = p.g;
     int32_t nxt[R];
     bool moved[R];
@@ -245,7 +175,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         // the label index holds CSR positions itself: no row pair to read
         if (S != kLabelIndex && s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
     }
-    if (Rec == kRecTable) {  // while the row pairs are in flight
+    if (kSparse) {  // while the row pairs are in flight
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -403,29 +333,20 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         if (s[r].widx < 0) continue;
-        if (!moved[r]) {
-            finish(p, s[r]);
-            if (Rec == kRecLog) log_release(p, lc);
-            continue;
-        }
+        if (!moved[r]) { finish(p, s[r]); continue; }
         s[r].prev = s[r].cur;
         if (S != kLabelIndex) s[r].prow = s[r].crow;  // (the label index reads no row pair)
         s[r].cur = nxt[r];
         if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
         s[r].len += 1;
         steps += 1;
-        if (Rec == kRecTable) {
+        if (kSparse) {
             const unsigned peers = __match_any_sync(__activemask(), ((unsigned long long)s[r].q << 32) | (uint32_t)nxt[r]);
             if ((threadIdx.x & 31) == __ffs(peers) - 1) start_insert(p, pend[r][0], s[r].q, nxt[r], __popc(peers));
-        } else if (Rec == kRecLog) {
-            log_visit(p, lc, nxt[r]);
         } else {
             record_visit(p, s[r].q, nxt[r]);
         }
-        if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) {
-            finish(p, s[r]);
-            if (Rec == kRecLog) log_release(p, lc);
-        }
+        if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) finish(p, s[r]);
     }
 }
 
@@ -436,13 +357,12 @@ __device__ __forceinline__ void flush_steps(const WalkParams &p, uint64_t steps)
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(p.steps, v);
 }
 
-template <int S, int U, int WK, int R, int Rec>
+template <int S, int U, int WK, int R, bool kSparse>
 __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams p) {
     const int lane = threadIdx.x & 31;
     constexpr unsigned long long kChunk = 32ull * R * 2;
     Slot s[R];
     PendingInsert pend[R][kInsertDepth];
-    const LogCtx lc{nullptr, 0};
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         s[r].widx = -1;
@@ -477,9 +397,9 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
 #pragma unroll
         for (int r = 0; r < R; ++r) live |= s[r].widx >= 0;
         if (!__any_sync(kFull, live)) break;
-        step_ring<S, U, WK, R, Rec>(p, s, steps, pend, lc);
+        step_ring<S, U, WK, R, kSparse>(p, s, steps, pend);
     }
-    if (Rec == kRecTable) {
+    if (kSparse) {
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -488,111 +408,17 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
     flush_steps(p, steps);
 }
 
-// Persistent engine for sparse PPR counts in log form (ring depth 1): a warp
-// claims whole items (kLogItem walkers of one query) from the queue head,
-// which here counts items, and admits their walkers as its lanes free up.
-// The warp's admission state is warp-uniform and packed into one word:
-// bits 0-6 next walker of the current item, 7-13 its walker count, 14-18
-// its ring slot, 19 "a current item exists", 20-24 the ring slot of the next
-// claim.
-template <int S>
-__global__ void __launch_bounds__(kThreadBlock, 6) walk_log(const WalkParams p, const int64_t num_items) {
-    __shared__ LogItem rings[kThreadBlock / 32][kLogRing];
-    const int lane = threadIdx.x & 31;
-    LogCtx lc{rings[threadIdx.x >> 5], 0};
-    lc.ring[lane].item = -1;  // kLogRing == 32: one ring slot per lane
-    lc.ring[lane].live = 0;
-    lc.ring[lane].admitted = 0;
-    __syncwarp();
-    Slot s[1];
-    s[0].widx = -1;
-    PendingInsert pend[1][kInsertDepth];
-    pend[0][0].q = -1;
-    uint64_t steps = 0;
-    int64_t r_first = 0;  // first walker of the current item
-    int32_t r_src = 0;    // its query's source
-    uint32_t st = 0;      // packed admission state (see above)
-    bool drained = false;
-    for (;;) {
-        unsigned need = __ballot_sync(kFull, s[0].widx < 0);
-        while (need && !drained) {
-            uint32_t r_next = st & 0x7Fu, r_end = (st >> 7) & 0x7Fu;
-            if (r_next >= r_end) {
-                if (st & (1u << 19)) {  // every walker of the current item is admitted
-                    if (lane == 0) {
-                        volatile LogItem &it = lc.ring[(st >> 14) & 31u];
-                        it.admitted = 1;
-                        __threadfence_block();
-                        if (atomicAdd((int *)&it.live, 0) == 0) log_close(p, it);
-                    }
-                    __syncwarp();
-                    st &= ~(1u << 19);
-                }
-                const uint32_t k = (st >> 20) & 31u;
-                // that ring slot still holds an item with a walker on this warp
-                // (kLogRing items ago): admit once it has finished
-                if (lc.ring[k].item >= 0) break;
-                unsigned long long b = 0;
-                if (lane == 0) b = atomicAdd(p.queue_head, 1ull);
-                b = __shfl_sync(kFull, b, 0);
-                if (b >= (unsigned long long)num_items) { drained = true; break; }
-                const int32_t q = (int32_t)(b / (uint32_t)p.items_per_query);
-                const int32_t c = (int32_t)(b - (unsigned long long)q * (uint32_t)p.items_per_query);
-                r_first = (int64_t)q * p.per_query + (int64_t)c * kLogItem;
-                r_src = __ldg(p.sources + q);
-                r_next = 0;
-                r_end = (uint32_t)min((int64_t)kLogItem, p.per_query - (int64_t)c * kLogItem);
-                st = r_end << 7 | k << 14 | 1u << 19 | ((k + 1) & 31u) << 20;
-                if (lane == 0) {
-                    volatile LogItem &it = lc.ring[k];
-                    for (int j = 0; j < kLogMaxSegs; ++j) it.fill[j] = 0;
-                    it.live = 0;
-                    it.admitted = 0;
-                    it.item = (int32_t)b;
-                }
-                __syncwarp();
-            }
-            const uint32_t slot = (st >> 14) & 31u;
-            const unsigned rank = __popc(need & lanemask_lt());
-            const bool mine = ((need >> lane) & 1u) && rank < r_end - r_next;
-            const unsigned took = __ballot_sync(kFull, mine);
-            if (lane == 0) atomicAdd((int *)&lc.ring[slot].live, __popc(took));
-            __syncwarp();
-            if (mine) {
-                lc.slot = (int32_t)slot;
-                s[0].widx = r_first + r_next + rank;
-                s[0].len = 1;
-                s[0].prev = -1;
-                s[0].prow = make_int2(0, 0);
-                s[0].cur = r_src;
-                if (r_src < 0 || r_src >= p.g.n) {  // rejected here so no kernel reads outside the graph
-                    atomicOr(p.error, kErrVertex);
-                    s[0].cur = 0;
-                    s[0].widx = -1;
-                    log_release(p, lc);
-                }
-            }
-            st += __popc(took);  // r_next
-            need &= ~took;
-        }
-        if (!__any_sync(kFull, s[0].widx >= 0)) break;
-        step_ring<S, kGeometric, kUnitWeight, 1, kRecLog>(p, s, steps, pend, lc);
-    }
-    flush_steps(p, steps);
-}
-
-template <int S, int U, int WK, int Rec>
+template <int S, int U, int WK, bool kSparse>
 __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t steps = 0;
     if (idx < p.num_walkers) {
         Slot s[1];
         PendingInsert pend[1][kInsertDepth];
-        const LogCtx lc{nullptr, 0};
-        for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
+            for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
         admit(p, s[0], idx);
-        while (s[0].widx >= 0) step_ring<S, U, WK, 1, Rec>(p, s, steps, pend, lc);
-        if (Rec == kRecTable)
+        while (s[0].widx >= 0) step_ring<S, U, WK, 1, kSparse>(p, s, steps, pend);
+        if (kSparse)
             for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[0][k], true);
     }
     flush_steps(p, steps);
@@ -605,59 +431,41 @@ int max_occupancy(K kernel) {
     return n;
 }
 
-template <int S, int U, int WK, int R, int Rec>
+template <int S, int U, int WK, int R, bool kSparse>
 cudaError_t launch_persistent(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
-    static const int max_occ = max_occupancy(walk_persistent<S, U, WK, R, Rec>);
+    static const int max_occ = max_occupancy(walk_persistent<S, U, WK, R, kSparse>);
     const int per_sm = shape.ctas_per_sm > 0 ? min(shape.ctas_per_sm, max_occ) : max_occ;
     int64_t grid = (int64_t)shape.num_sms * per_sm;
     const int64_t useful = (p.num_walkers + (int64_t)kThreadBlock * R - 1) / ((int64_t)kThreadBlock * R);
     if (useful < grid) grid = useful;
     if (grid <= 0) return cudaSuccess;
-    walk_persistent<S, U, WK, R, Rec><<<(unsigned)grid, kThreadBlock, 0, st>>>(p);
+    walk_persistent<S, U, WK, R, kSparse><<<(unsigned)grid, kThreadBlock, 0, st>>>(p);
     return cudaGetLastError();
 }
 
-template <int S>
-cudaError_t launch_log(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
-    static const int max_occ = max_occupancy(walk_log<S>);
-    const int per_sm = shape.ctas_per_sm > 0 ? min(shape.ctas_per_sm, max_occ) : max_occ;
-    int64_t grid = (int64_t)shape.num_sms * per_sm;
-    const int64_t useful = (p.num_walkers + kThreadBlock - 1) / kThreadBlock;
-    if (useful < grid) grid = useful;
-    if (grid <= 0 || p.per_query <= 0) return cudaSuccess;
-    const int64_t num_items = p.num_walkers / p.per_query * p.items_per_query;
-    walk_log<S><<<(unsigned)grid, kThreadBlock, 0, st>>>(p, num_items);
-    return cudaGetLastError();
-}
-
-template <int S, int U, int WK, int Rec>
+template <int S, int U, int WK, bool kSparse>
 cudaError_t launch_mode(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
     if (shape.engine == kEnginePlain) {
         const int64_t blocks = (p.num_walkers + kThreadBlock - 1) / kThreadBlock;
         if (blocks <= 0) return cudaSuccess;
-        walk_plain<S, U, WK, Rec><<<(unsigned)blocks, kThreadBlock, 0, st>>>(p);
+        walk_plain<S, U, WK, kSparse><<<(unsigned)blocks, kThreadBlock, 0, st>>>(p);
         return cudaGetLastError();
     }
     switch (shape.ring) {
-    case 1: return launch_persistent<S, U, WK, 1, Rec>(p, shape, st);
-    case 2: return launch_persistent<S, U, WK, 2, Rec>(p, shape, st);
-    case 8: return launch_persistent<S, U, WK, 8, Rec>(p, shape, st);
-    default: return launch_persistent<S, U, WK, 4, Rec>(p, shape, st);
+    case 1: return launch_persistent<S, U, WK, 1, kSparse>(p, shape, st);
+    case 2: return launch_persistent<S, U, WK, 2, kSparse>(p, shape, st);
+    case 8: return launch_persistent<S, U, WK, 8, kSparse>(p, shape, st);
+    default: return launch_persistent<S, U, WK, 4, kSparse>(p, shape, st);
     }
 }
 
-// Sparse visit counts only exist for PPR (geometric update, unit weights):
-// the log form on the persistent engine, the table form otherwise.
+// Sparse visit tables only exist for PPR (geometric update).
 template <int S, int U, int WK>
 cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStream_t st) {
-    if constexpr (U == kGeometric && WK == kUnitWeight) {
-        if (p.log) {
-            if (shape.engine == kEnginePlain) return cudaErrorInvalidValue;
-            return launch_log<S>(p, shape, st);
-        }
-        if (p.table) return launch_mode<S, U, WK, kRecTable>(p, shape, st);
+    if constexpr (U == kGeometric) {
+        if (p.table) return launch_mode<S, U, WK, true>(p, shape, st);
     }
-    return launch_mode<S, U, WK, kRecCounts>(p, shape, st);
+    return launch_mode<S, U, WK, false>(p, shape, st);
 }
 
 }  // namespace
