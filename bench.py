@@ -53,12 +53,13 @@ BYTES_PER_STEP = {
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per step of each
 # workload's walk kernel, from one ncu capture of that kernel: PPR on the
-# full N = 2^22 graph with 256 queries (the full batch's tables do not change
-# the per-step traffic of the walk: only the in-flight queries' tables are
-# written), the others on their full graphs with a reduced walker count.
-# Scaled by the steps of one full launch.
+# full N = 2^22 graph with 256 queries (1.386 GB over 12.80 M steps; the full
+# batch's tables do not change the per-step traffic of the walk: only the
+# in-flight queries' tables are written), DeepWalk on its full graph, Node2Vec
+# and MetaPath on R-MAT 2^22 instances of their graphs.  Scaled by the steps
+# of one full launch.
 TRAFFIC_BYTES_PER_STEP = {
-    "ppr": 70.73,
+    "ppr": 108.25,
     "ppr_dense": 89.13,
     "deepwalk": 16.47,
     "node2vec": 274.7,
@@ -88,7 +89,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ppr", choices=sorted(WORKLOADS) + ["serving"])
-    ap.add_argument("--rates", default="50,200,800", help="serving: arrival rates (requests/s)")
+    ap.add_argument("--rates", default="50,200,800,1600,3200", help="serving: arrival rates (requests/s)")
+    ap.add_argument("--inflight", type=int, default=4, help="serving: batches in flight (streams)")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--queries", type=int, default=None, help="override the query count (small runs)")
     ap.add_argument("--scale", type=int, default=None, help="override log2(N) (small runs)")
@@ -704,10 +706,13 @@ def run_ours(args):
 
 def run_serving(args):
     """Serving mix: Poisson arrivals at swept rates on a resident R-MAT graph
-    (alias + ITS tables, edge set and label index built), apps uniform over PPR / DeepWalk / Node2Vec /
-    MetaPath, walkers log-uniform in [1e3, 1e6], lengths uniform in [5, 80].
-    Reports p50 / p99 latency (submit -> results complete in HBM) and steps/s
-    per arrival rate."""
+    (alias + ITS tables, edge set and label index built), apps uniform over
+    PPR / DeepWalk / Node2Vec / MetaPath, walkers log-uniform in [1e3, 1e6],
+    lengths uniform in [5, 80].  Per rate: offered and achieved request rates,
+    steps/s, p50 / p99 latency (submit -> results complete in HBM) and the
+    number of batches (persistent launches per kernel) the loop formed.
+    Sources come from one pool of random non-isolated vertices drawn once,
+    so submitting a request costs no sampling on the host."""
     import torch
     from thunderrw_gb300 import engine as E
     from thunderrw_gb300 import generators as G
@@ -717,7 +722,7 @@ def run_serving(args):
     scale = args.scale or 25
     g = G.make_graph("rmat", 1 << scale, 32, seed=20240601, device="cuda", labels=5)
     graph = E.Graph(g["row"], g["adj"], g["weight"], g["label"])
-    nz = torch.nonzero(g["row"][1:] - g["row"][:-1]).flatten().to(torch.int32).cpu().numpy()
+    pool = G.random_sources(g["row"], 1 << 22, seed=17).cpu().numpy()
     del g
     torch.cuda.empty_cache()
     t0 = time.perf_counter()
@@ -727,9 +732,17 @@ def run_serving(args):
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     rng = np.random.default_rng(5)
+    apps = [None, E.DeepWalk, lambda L: E.Node2Vec(L, 2.0, 0.5), lambda L: E.MetaPath(L, [0, 1, 2, 3, 4])]
     results = []
     for rate in [float(x) for x in args.rates.split(",")]:
-        srv = Server(graph, max_inflight=8)
+        n = int(rate * args.serve_seconds) + 1
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+        kinds = rng.integers(0, 4, size=n)
+        walkers = np.exp(rng.uniform(np.log(1e3), np.log(1e6), size=n)).astype(np.int64)
+        lengths = rng.integers(5, 81, size=n)
+        starts = rng.integers(0, pool.size - 1_000_000, size=n)
+        seeds = rng.integers(1, 1 << 62, size=n)
+        srv = Server(graph, max_inflight=args.inflight)
         tickets = []
         done = threading.Event()
 
@@ -741,38 +754,39 @@ def run_serving(args):
                     srv.release(tickets[i])
                     i += 1
                 else:
-                    time.sleep(0.0005)
+                    time.sleep(0.0002)
 
         th = threading.Thread(target=collector)
         th.start()
         t_start = time.perf_counter()
-        nreq = 0
-        while time.perf_counter() - t_start < args.serve_seconds:
-            kind = rng.integers(0, 4)
-            walkers = int(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
-            length = int(rng.integers(5, 81))
-            seed = int(rng.integers(1, 1 << 62))
-            if kind == 0:
-                tickets.append(srv.submit_ppr(rng.choice(nz, size=1), walkers, tp=0.2, seed=seed))
+        for i in range(n):
+            while time.perf_counter() - t_start < arrivals[i]:
+                pass
+            k = int(kinds[i])
+            if k == 0:
+                tickets.append(srv.submit_ppr(pool[starts[i]:starts[i] + 1], int(walkers[i]), tp=0.2, seed=int(seeds[i])))
             else:
-                app = [None, E.DeepWalk(length), E.Node2Vec(length, 2.0, 0.5), E.MetaPath(length, [0, 1, 2, 3, 4])][kind]
-                tickets.append(srv.submit_walk(app, rng.choice(nz, size=walkers), seed=seed))
-            nreq += 1
-            time.sleep(rng.exponential(1.0 / rate))
+                tickets.append(srv.submit_walk(apps[k](int(lengths[i])), pool[starts[i]:starts[i] + int(walkers[i])],
+                                               seed=int(seeds[i])))
+        offered_s = time.perf_counter() - t_start
         done.set()
         th.join()
         st = srv.stats()
         srv.stop()
-        results.append({"rate_req_s": rate, "requests": nreq, "completed": st["completed"], "failed": st["failed"],
-                        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+        results.append({"rate_req_s": rate, "requests": n, "offered_req_s": n / offered_s,
+                        "achieved_req_s": st["completed"] / st["elapsed_s"], "completed": st["completed"],
+                        "failed": st["failed"], "batches": st["batches"], "p50_ms": st["p50_ms"],
+                        "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
                         "steps_per_s": st["steps"] / st["elapsed_s"], "elapsed_s": st["elapsed_s"]})
         print(json.dumps(results[-1]), file=sys.stderr, flush=True)
     best = max(results, key=lambda r: r["steps_per_s"])
     line = {"metric": "walk_steps_per_s", "value": best["steps_per_s"], "unit": "steps/s", "n_gpus": 1,
             "steps": len(results), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+f64", "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": "serving mix rmat N=2^%d deg=32, 5 labels, alias+ITS tables, edge set and label index resident" % scale,
-                       "n": graph.n, "e": graph.e, "table_build_s": build_s,
+            "config": {"workload": "serving mix rmat N=2^%d deg=32, 5 labels, alias+ITS tables, edge set and label "
+                                   "index resident; PPR/DeepWalk/Node2Vec/MetaPath uniform, walkers log-uniform "
+                                   "1e3-1e6, L 5-80, Poisson arrivals" % scale,
+                       "n": graph.n, "e": graph.e, "table_build_s": build_s, "max_inflight": args.inflight,
                        "indexes": {"edge_set": indexes[0], "label_index": indexes[1]}},
             "serving": results}
     print(json.dumps(line), flush=True)

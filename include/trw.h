@@ -287,6 +287,7 @@ typedef struct {
     int64_t queued, running;
     size_t hbm_in_use;
     double p50_ms, p99_ms, max_ms, elapsed_s;
+    uint64_t batches;    /* batches launched (each: one persistent launch per kernel of its requests) */
 } trw_serving_stats;
 
 int trw_server_start(trw_graph *g, size_t hbm_budget_bytes, int32_t max_inflight, trw_server **out);

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "trw.h"
+#include "trw_batch.h"
 #include "trw_device.cuh"
 #include "trw_internal.h"
 
@@ -472,22 +473,10 @@ int ensure_host_pipeline(trw_graph *g) {
     return TRW_OK;
 }
 
-// Shared implementation of trw_walk and trw_ppr_batch.
-int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
-             int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
-             int32_t *lengths, int32_t *counts, int64_t counts_len, bool zero_counts, uint64_t *steps,
-             int32_t engine, cudaStream_t st, int32_t *table = nullptr, int32_t table_bits = 0,
-             bool hold_lock = false) {
-    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
-    if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
-    if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
-    if (engine != TRW_ENGINE_PERSISTENT && engine != TRW_ENGINE_PLAIN) return fail(TRW_ERR_INVALID, "bad engine");
-    Plan pl;
-    int rc = make_plan(g, desc, pl);
-    if (rc) return rc;
-    std::unique_lock<std::mutex> lock(g->mu, std::defer_lock);
-    if (!hold_lock) lock.lock();
-    TRW_CUDA(cudaSetDevice(g->device));
+// The kernel a walk runs and the graph structures it needs, built on first
+// use (the caller holds the graph lock and has made the device current).
+int prepare_plan(trw_graph *g, const trw_walk_desc *desc, Plan &pl, cudaStream_t st) {
+    int rc = TRW_OK;
     // Dynamic mode with walker-independent weights (DeepWalk and GenericWalk:
     // edge weights; PPR: 1) gathers the same row every step, so its per-step
     // ITS prefix, alias table or row maximum is the static one (same builder
@@ -531,6 +520,28 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
             pl.sampler = kLabelIndex;
         }
     }
+
+    return TRW_OK;
+}
+
+// Shared implementation of trw_walk and trw_ppr_batch.
+int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_sources,
+             int64_t num_walkers, int64_t per_query, int64_t id_base, int32_t *paths, int32_t path_cap,
+             int32_t *lengths, int32_t *counts, int64_t counts_len, bool zero_counts, uint64_t *steps,
+             int32_t engine, cudaStream_t st, int32_t *table = nullptr, int32_t table_bits = 0,
+             bool hold_lock = false) {
+    if (!g || !desc) return fail(TRW_ERR_INVALID, "null graph or descriptor");
+    if (num_walkers < 0 || (num_walkers > 0 && !sources)) return fail(TRW_ERR_INVALID, "bad walker arguments");
+    if (paths && path_cap <= 0) return fail(TRW_ERR_INVALID, "path_cap must be > 0 when paths are requested");
+    if (engine != TRW_ENGINE_PERSISTENT && engine != TRW_ENGINE_PLAIN) return fail(TRW_ERR_INVALID, "bad engine");
+    Plan pl;
+    int rc = make_plan(g, desc, pl);
+    if (rc) return rc;
+    std::unique_lock<std::mutex> lock(g->mu, std::defer_lock);
+    if (!hold_lock) lock.lock();
+    TRW_CUDA(cudaSetDevice(g->device));
+    rc = prepare_plan(g, desc, pl, st);
+    if (rc) return rc;
 
     // Stage host buffers.
     const bool h_src = sources && !is_device_ptr(sources);
@@ -1132,6 +1143,141 @@ int trw_device_error(trw_graph *g, int32_t *code) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched walks of the serving loop (trw_batch.h).
+// ---------------------------------------------------------------------------
+
+int32_t trw::batch_ppr_bits(const trw_graph *g, int64_t walkers, double tp) {
+    // as trw_ppr_batch_sparse: 2^bits >= 1.25 x the expected visits, <= 2 n
+    const double visits = (double)walkers / tp;
+    int32_t bits = 10;
+    while (bits < 30 && (double)(1ll << bits) < 1.25 * visits) ++bits;
+    while (bits > 10 && (1ll << (bits - 1)) >= 2ll * g->n) --bits;
+    return bits;
+}
+
+int64_t trw::batch_ppr_distinct_ints(int32_t bits) { return ppr_distinct_ints(bits); }
+
+int trw::batch_walk(trw_graph *g, std::vector<BatchItem> &items, cudaStream_t st, std::vector<int> &host_done) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    host_done.clear();
+    // plan every request; group the thread-engine ones by kernel
+    struct Key {
+        int sampler, update, wk;
+        bool operator<(const Key &o) const {
+            return sampler != o.sampler ? sampler < o.sampler : update != o.update ? update < o.update : wk < o.wk;
+        }
+    };
+    std::vector<std::pair<Key, int>> shared;
+    std::vector<int> alone;
+    std::vector<Plan> plans(items.size());
+    for (int i = 0; i < (int)items.size(); ++i) {
+        BatchItem &it = items[(size_t)i];
+        Plan &pl = plans[(size_t)i];
+        int rc = make_plan(g, &it.desc, pl);
+        if (rc) return rc;
+        rc = prepare_plan(g, &it.desc, pl, st);
+        if (rc) return rc;
+        if (it.num_walkers <= 0) { host_done.push_back(i); continue; }
+        if (pl.warp_family) alone.push_back(i);
+        else shared.push_back({Key{pl.sampler, pl.update, pl.weight_kind}, i});
+    }
+    std::stable_sort(shared.begin(), shared.end(),
+                     [](const std::pair<Key, int> &a, const std::pair<Key, int> &b) { return a.first < b.first; });
+    for (size_t a = 0; a < shared.size();) {
+        size_t b = a;
+        while (b < shared.size() && !(shared[a].first < shared[b].first) && !(shared[b].first < shared[a].first)) ++b;
+        const Key key = shared[a].first;
+        const int k = (int)(b - a);
+        // device request table: parameters, chunk prefix, PPR tables and
+        // table sizes, walkers left, completion flags, queue head
+        const size_t b_p = align_up(sizeof(WalkParams) * (size_t)k);
+        const size_t b_c = align_up(sizeof(int64_t) * (size_t)(k + 1));
+        const size_t b_t = align_up(sizeof(int32_t *) * (size_t)k);
+        const size_t b_b = align_up(sizeof(int32_t) * (size_t)k);
+        const size_t b_r = align_up(sizeof(int32_t) * (size_t)k);
+        const size_t b_d = align_up(sizeof(int32_t *) * (size_t)k);
+        const size_t bytes = b_p + b_c + b_t + b_b + b_r + b_d + sizeof(unsigned long long);
+        std::vector<char> h(bytes, 0);
+        WalkParams *hp = reinterpret_cast<WalkParams *>(h.data());
+        int64_t *hc = reinterpret_cast<int64_t *>(h.data() + b_p);
+        int32_t **ht = reinterpret_cast<int32_t **>(h.data() + b_p + b_c);
+        int32_t *hb = reinterpret_cast<int32_t *>(h.data() + b_p + b_c + b_t);
+        int32_t *hr = reinterpret_cast<int32_t *>(h.data() + b_p + b_c + b_t + b_b);
+        volatile int32_t **hd = reinterpret_cast<volatile int32_t **>(h.data() + b_p + b_c + b_t + b_b + b_r);
+        bool any_table = false;
+        int64_t walkers = 0;
+        hc[0] = 0;
+        for (int j = 0; j < k; ++j) {
+            const BatchItem &it = items[(size_t)shared[a + (size_t)j].second];
+            const Plan &pl = plans[(size_t)shared[a + (size_t)j].second];
+            WalkParams &p = hp[j];
+            p.g = dev_view(g);
+            fill_app_params(p, &it.desc);
+            p.static_unit = pl.table_kind == TRW_WEIGHTS_UNIT;
+            p.sources = it.sources;
+            p.num_walkers = it.num_walkers;
+            p.per_query = it.per_query;
+            p.id_base = it.id_base;
+            p.paths = it.paths;
+            p.path_cap = it.paths ? it.path_cap : 0;
+            p.lengths = it.lengths;
+            p.steps = reinterpret_cast<unsigned long long *>(it.steps);
+            p.error = g->error;
+            hc[j + 1] = hc[j] + (it.num_walkers + kMultiChunk - 1) / kMultiChunk;
+            ht[j] = it.table;
+            hb[j] = it.table_bits;
+            hr[j] = (int32_t)it.num_walkers;
+            hd[j] = it.table ? nullptr : it.done;  // PPR requests finish after their post-processing
+            any_table |= it.table != nullptr;
+            walkers += it.num_walkers;
+        }
+        char *d = nullptr;
+        TRW_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, st));
+        // from pageable memory: the call returns once `h` has been staged
+        TRW_CUDA(cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, st));
+        MultiBatch mb;
+        mb.reqs = reinterpret_cast<const WalkParams *>(d);
+        mb.chunk_start = reinterpret_cast<const int64_t *>(d + b_p);
+        mb.nreq = k;
+        mb.tables = any_table ? reinterpret_cast<int32_t *const *>(d + b_p + b_c) : nullptr;
+        mb.table_bits = reinterpret_cast<const int32_t *>(d + b_p + b_c + b_t);
+        mb.remaining = reinterpret_cast<int32_t *>(d + b_p + b_c + b_t + b_b);
+        mb.done = reinterpret_cast<volatile int32_t *const *>(d + b_p + b_c + b_t + b_b + b_r);
+        mb.queue_head = reinterpret_cast<unsigned long long *>(d + b_p + b_c + b_t + b_b + b_r + b_d);
+        mb.error = g->error;
+        const cudaError_t le = launch_walk_multi(mb, walkers, hc[k], key.sampler, key.update, key.wk, g->num_sms, st);
+        if (le != cudaSuccess) return fail(TRW_ERR_CUDA, "batched walk launch: %s", cudaGetErrorString(le));
+        TRW_CUDA(cudaFreeAsync(d, st));
+        for (int j = 0; j < k; ++j) {
+            const int i = shared[a + (size_t)j].second;
+            if (!items[(size_t)i].done || items[(size_t)i].table) host_done.push_back(i);
+        }
+        a = b;
+    }
+    for (int i : alone) {
+        BatchItem &it = items[(size_t)i];
+        const int rc = run_walk(g, &it.desc, it.sources, it.per_query > 0 ? it.num_walkers / it.per_query : it.num_walkers,
+                                it.num_walkers, it.per_query, it.id_base, it.paths,
+                                it.path_cap, it.lengths, nullptr, 0, false, it.steps, TRW_ENGINE_PERSISTENT, st,
+                                nullptr, 0, /*hold_lock=*/true);
+        if (rc) return rc;
+        host_done.push_back(i);
+    }
+    // single-query PPR requests: their table into CSR
+    for (BatchItem &it : items) {
+        if (!it.table) continue;
+        TRW_CUDA(cudaMemsetAsync(it.offsets, 0, sizeof(int64_t), st));
+        TRW_CUDA(launch_ppr_offsets(it.table, it.table_bits, it.distinct, 1, it.offsets, st));
+        TRW_CUDA(launch_ppr_emit(it.table, it.table_bits, 1, it.offsets, it.distinct, it.vertices, it.counts,
+                                 it.capacity, g->error, st));
+    }
+    std::sort(host_done.begin(), host_done.end());
+    return TRW_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Dynamic-alias walks that allocate nothing.

@@ -28,6 +28,30 @@ cudaError_t launch_walk_warp(const WalkParams &p, int sampler, int update, int w
 // number of per-warp dynamic-alias scratch tables the warp engine will use
 int64_t warp_engine_warps(const WalkParams &p, const LaunchShape &shape);
 
+// Many requests in one persistent launch (the serving loop's batches): the
+// walkers of all requests share one queue of chunks of kMultiChunk walkers,
+// request r owning chunks [chunk_start[r], chunk_start[r + 1]).  reqs[r]
+// holds request r's parameters with no visit-count outputs; a request with
+// tables[r] != null (single-query PPR) records its visits in that
+// 2^table_bits[r]-slot table (the layout of WalkParams::table).  remaining[r]
+// starts at the request's walker count; the lane that finishes its last
+// walker writes 1 to *done[r] (host-mapped memory) if done[r] is set.  All
+// requests share the sampler, update rule and weight kind of the launch.
+constexpr int kMultiChunk = 64;
+struct MultiBatch {
+    const WalkParams *reqs;
+    const int64_t *chunk_start;
+    int32_t nreq;
+    int32_t *const *tables;
+    const int32_t *table_bits;
+    int32_t *remaining;
+    volatile int32_t *const *done;
+    unsigned long long *queue_head;
+    int *error;
+};
+cudaError_t launch_walk_multi(const MultiBatch &mb, int64_t total_walkers, int64_t total_chunks, int sampler,
+                              int update, int weight_kind, int num_sms, cudaStream_t st);
+
 // offsets[0] must hold the entries before this range of queries (0 for the first)
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
                                cudaStream_t st);

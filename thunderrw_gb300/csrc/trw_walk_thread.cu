@@ -424,6 +424,100 @@ __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
     flush_steps(p, steps);
 }
 
+// Multi-request form of the persistent engine (ring depth 1, the serving
+// loop's batches): a warp claims chunks of kMultiChunk walkers of one request
+// from the shared queue (the admission of creeper.h:321-332 over many
+// requests' walkers), and each lane steps its walker with its own request's
+// parameters (read through L1 from the request table).  PPR requests record
+// each move in their own table, lanes of the warp on the same (request,
+// vertex) merged first; each finished walker adds its moves to its
+// request's step counter, and the lane that finishes a request's last walker
+// raises the request's completion flag in host memory.
+template <int S, int U, int WK>
+__global__ void __launch_bounds__(kThreadBlock) walk_multi(const MultiBatch mb, const int64_t total_chunks) {
+    const int lane = threadIdx.x & 31;
+    Slot s[1];
+    s[0].widx = -1;
+    PendingInsert pend[1][kInsertDepth];
+    pend[0][0].q = -1;
+    int32_t req = 0;      // this lane's walker's request
+    uint32_t wsteps = 0;  // its moves so far
+    int32_t r_req = 0;    // the warp's current chunk: request, next walker, end
+    int64_t r_next = 0, r_end = 0;
+    bool drained = false;
+    for (;;) {
+        unsigned need = __ballot_sync(kFull, s[0].widx < 0);
+        while (need && !drained) {
+            if (r_next >= r_end) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(mb.queue_head, 1ull);
+                b = __shfl_sync(kFull, b, 0);
+                if (b >= (unsigned long long)total_chunks) { drained = true; break; }
+                int32_t lo = 0, hi = mb.nreq;  // request r with chunk_start[r] <= b < chunk_start[r + 1]
+                while (hi - lo > 1) {
+                    const int32_t mid = (lo + hi) >> 1;
+                    if (__ldg(mb.chunk_start + mid) <= (int64_t)b) lo = mid; else hi = mid;
+                }
+                r_req = lo;
+                r_next = ((int64_t)b - __ldg(mb.chunk_start + lo)) * kMultiChunk;
+                r_end = min(r_next + kMultiChunk, mb.reqs[lo].num_walkers);
+            }
+            const unsigned avail = (unsigned)min(r_end - r_next, (int64_t)32);
+            const unsigned rank = __popc(need & lanemask_lt());
+            const bool mine = ((need >> lane) & 1u) && rank < avail;
+            bool dead = false;
+            if (mine) {
+                req = r_req;
+                wsteps = 0;
+                admit(mb.reqs[req], s[0], r_next + rank);
+                dead = s[0].widx < 0;  // an invalid source finishes at once
+            }
+            if (dead) {
+                __threadfence();
+                const unsigned peers = __match_any_sync(__activemask(), req);
+                if (lane == __ffs(peers) - 1) {
+                    const int n = __popc(peers);
+                    if (atomicSub(mb.remaining + req, n) == n && mb.done[req]) {
+                        __threadfence_system();
+                        *mb.done[req] = 1;
+                    }
+                }
+            }
+            r_next += min((unsigned)__popc(need), avail);
+            need &= ~__ballot_sync(kFull, mine);
+        }
+        if (!__any_sync(kFull, s[0].widx >= 0)) break;
+        const WalkParams &p = mb.reqs[req];
+        const bool was = s[0].widx >= 0;
+        const int32_t len0 = s[0].len;
+        uint64_t moved = 0;
+        step_ring<S, U, WK, 1, false>(p, s, moved, pend);
+        wsteps += (uint32_t)moved;
+        if (mb.tables && was && s[0].len != len0) {  // a PPR move to s[0].cur
+            int32_t *t = mb.tables[req];
+            if (t) {
+                const unsigned peers =
+                    __match_any_sync(__activemask(), ((unsigned long long)(uint32_t)req << 32) | (uint32_t)s[0].cur);
+                if (lane == __ffs(peers) - 1) table_add(t, mb.table_bits[req], s[0].cur, __popc(peers), mb.error);
+            }
+        }
+        if (was && s[0].widx < 0) {  // the walker finished
+            const unsigned peers = __match_any_sync(__activemask(), req);
+            const unsigned total = __reduce_add_sync(peers, wsteps);
+            __threadfence();  // this group's outputs and moves before the countdown
+            if (lane == __ffs(peers) - 1) {
+                atomicAdd(p.steps, (unsigned long long)total);
+                __threadfence();
+                const int n = __popc(peers);
+                if (atomicSub(mb.remaining + req, n) == n && mb.done[req]) {
+                    __threadfence_system();
+                    *mb.done[req] = 1;
+                }
+            }
+        }
+    }
+}
+
 template <class K>
 int max_occupancy(K kernel) {
     int n = 0;
@@ -468,7 +562,44 @@ cudaError_t launch_shape(const WalkParams &p, const LaunchShape &shape, cudaStre
     return launch_mode<S, U, WK, false>(p, shape, st);
 }
 
+template <int S, int U, int WK>
+cudaError_t launch_multi(const MultiBatch &mb, int64_t total_walkers, int64_t total_chunks, int num_sms,
+                         cudaStream_t st) {
+    static const int max_occ = max_occupancy(walk_multi<S, U, WK>);
+    int64_t grid = (int64_t)num_sms * max_occ;
+    const int64_t useful = (total_walkers + kThreadBlock - 1) / kThreadBlock;
+    if (useful < grid) grid = useful;
+    if (grid <= 0 || mb.nreq <= 0 || total_chunks <= 0) return cudaSuccess;
+    walk_multi<S, U, WK><<<(unsigned)grid, kThreadBlock, 0, st>>>(mb, total_chunks);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_walk_multi(const MultiBatch &mb, int64_t total_walkers, int64_t total_chunks, int sampler,
+                              int update, int weight_kind, int num_sms, cudaStream_t st) {
+    const bool geo = update == kGeometric;
+    switch (sampler) {
+    case kUniform: return geo ? launch_multi<kUniform, kGeometric, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st)
+                              : launch_multi<kUniform, kFixedLength, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st);
+    case kAlias: return geo ? launch_multi<kAlias, kGeometric, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st)
+                            : launch_multi<kAlias, kFixedLength, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st);
+    case kITS: return geo ? launch_multi<kITS, kGeometric, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st)
+                          : launch_multi<kITS, kFixedLength, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st);
+    case kRejection:
+        return geo ? launch_multi<kRejection, kGeometric, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st)
+                   : launch_multi<kRejection, kFixedLength, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st);
+    case kLabelIndex: return launch_multi<kLabelIndex, kFixedLength, kLabelSchema>(mb, total_walkers, total_chunks, num_sms, st);
+    case kMaxRejection:
+        if (weight_kind == kNode2Vec)
+            return launch_multi<kMaxRejection, kFixedLength, kNode2Vec>(mb, total_walkers, total_chunks, num_sms, st);
+        if (weight_kind == kEdgeWeight)
+            return launch_multi<kMaxRejection, kFixedLength, kEdgeWeight>(mb, total_walkers, total_chunks, num_sms, st);
+        if (geo) return launch_multi<kMaxRejection, kGeometric, kUnitWeight>(mb, total_walkers, total_chunks, num_sms, st);
+        return cudaErrorInvalidValue;
+    }
+    return cudaErrorInvalidValue;
+}
 
 cudaError_t launch_walk_thread(const WalkParams &p, int sampler, int update, int weight_kind,
                                const LaunchShape &shape, cudaStream_t st) {

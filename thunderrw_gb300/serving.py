@@ -32,7 +32,7 @@ class _Stats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("steps", ctypes.c_uint64), ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
                 ("hbm_in_use", ctypes.c_size_t), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
-                ("max_ms", ctypes.c_double), ("elapsed_s", ctypes.c_double)]
+                ("max_ms", ctypes.c_double), ("elapsed_s", ctypes.c_double), ("batches", ctypes.c_uint64)]
 
 
 def _bind():
