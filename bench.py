@@ -62,7 +62,7 @@ TRAFFIC_BYTES_PER_STEP = {
     "ppr": 108.25,
     "ppr_dense": 89.13,
     "deepwalk": 16.47,
-    "node2vec": 274.7,
+    "node2vec": 198.29,
     "metapath": 155.1,
 }
 
@@ -629,8 +629,9 @@ def measure(name, args, over, dev, rank, world, steps, warmup, headline):
         # Algorithmic bytes per move of the timed walks (the last batch's
         # paths, first 65536 walkers) under the kernel's own access pattern.
         sample = paths[:65536].cpu().numpy()
-        if name == "node2vec":
-            bps = bytes_model.node2vec(sample, wl["length"])
+        if name == "node2vec":  # probes only where the kernel makes them (its draws, from the seed)
+            bps = bytes_model.node2vec(sample, wl["length"], seed=replicas.replica_seed(2000 + steps - 1, rank),
+                                       p=wl["p"], q=wl["q"])
         elif graph.indexes()[1] == 1:  # MetaPath answered from the label index
             bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"])
         else:

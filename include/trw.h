@@ -258,10 +258,14 @@ int trw_profile_read(trw_graph *g, float *walk_ms, float *post_ms);
 
 /* A request loop over a resident graph (no counterpart in the reference,
  * which runs one compute() per process).  Requests of any app and size are
- * admitted in arrival order whenever one of `max_inflight` streams is free and
- * the request's device memory fits `hbm_budget_bytes` (0 = 80 % of the free
- * HBM at start); each admitted request runs on its own stream, overlapping the
- * ones already running.  Results stay in HBM until trw_server_release. */
+ * admitted in arrival order: whenever one of `max_inflight` streams is free,
+ * every queued request whose device memory still fits `hbm_budget_bytes` (0 =
+ * 80 % of the free HBM at start) joins one batch on that stream, and the
+ * walkers of the batch's requests that use the same kernel run in one shared
+ * persistent launch (one work queue over all of them).  Batches on different
+ * streams overlap on the device.  A request completes when its last walker
+ * does (single-query PPR requests: when their post-processing does).
+ * Results stay in HBM until trw_server_release. */
 typedef struct trw_server trw_server;
 
 typedef struct {

@@ -89,3 +89,29 @@ def test_sector_reuse_counts_hot_sectors():
     assert 0.0 < out["row_pair_hit_1KB"] <= 1.0
     share = B.top_degree_share(r["paths"], row, ks=(1, 4096))
     assert share[4096] == 1.0 and share[1] > 0.0  # every walk starts at the highest-degree vertex
+
+
+def test_philox_restatement_matches_oracle():
+    """The byte model's vectorised Philox4x32-10 gives the oracle's words."""
+    from thunderrw_gb300 import bytes_model as B
+    for seed, w, st, blk in [(1, 0, 1, 0), (12345678901, 77, 5, 0), (2**63 + 5, 2**33 + 9, 79, 3),
+                             (7, 1 << 20, 2, 0x80000000)]:
+        ref = O.philox([blk, st, w & 0xFFFFFFFF, w >> 32], [seed & 0xFFFFFFFF, seed >> 32])
+        got = [int(B.philox_word(seed, np.array([w]), np.array([st]), blk, i)[0]) for i in range(4)]
+        assert got == [int(x) for x in ref]
+    assert B.accept_threshold(2.0, 1.0) == 1 << 31
+    assert B.accept_threshold(2.0, 2.0) == 0xFFFFFFFF
+
+
+def test_node2vec_model_charges_probes_only_in_the_band():
+    """With the seed, moves whose first acceptance draw lies at or below the
+    lower threshold are not charged a probe: fewer bytes than the plain count."""
+    from thunderrw_gb300 import bytes_model as B
+    g = G.make_graph("rmat", 1 << 11, 8, seed=4, weights=False)
+    og = O.Graph(g["row"].numpy(), g["adj"].numpy())
+    src = G.all_sources(g["row"], seed=1).numpy()[:500]
+    r = O.walk(og, O.make_desc("node2vec", "dynamic", "maxweight_rejection", length=20, p=2.0, q=0.5, seed=9), src,
+               path_cap=20)
+    full = B.node2vec(r["paths"], 20)
+    lazy = B.node2vec(r["paths"], 20, seed=9, p=2.0, q=0.5)
+    assert 68.0 < lazy < full

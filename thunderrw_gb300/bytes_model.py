@@ -55,19 +55,64 @@ def _stops(paths: np.ndarray, length: int):
     return np.asarray(paths)[early, n_entries[early] - 1]
 
 
-def node2vec(paths: np.ndarray, length: int) -> float:
+def philox_word(seed: int, walker: np.ndarray, step: np.ndarray, block: int, word: int) -> np.ndarray:
+    """Word `word` of Philox4x32-10 (Salmon et al., SC'11) with key = seed and
+    counter = (block, step, walker lo, walker hi): the engine's draw stream,
+    vectorised over walkers and steps."""
+    m = np.uint64(0xFFFFFFFF)
+    walker = np.asarray(walker, dtype=np.uint64)
+    c0 = np.full(walker.shape, block, dtype=np.uint64)
+    c1 = np.asarray(step, dtype=np.uint64) & m
+    c2 = walker & m
+    c3 = walker >> np.uint64(32)
+    k0, k1 = np.uint64(seed & 0xFFFFFFFF), np.uint64((seed >> 32) & 0xFFFFFFFF)
+    for r in range(10):
+        if r:
+            k0 = (k0 + np.uint64(0x9E3779B9)) & m
+            k1 = (k1 + np.uint64(0xBB67AE85)) & m
+        p0 = np.uint64(0xD2511F53) * c0
+        p1 = np.uint64(0xCD9E8D57) * c2
+        c0, c1, c2, c3 = ((p1 >> np.uint64(32)) ^ c1 ^ k0) & m, p1 & m, ((p0 >> np.uint64(32)) ^ c3 ^ k1) & m, p0 & m
+    return (c0, c1, c2, c3)[word].astype(np.uint32)
+
+
+def accept_threshold(max_weight: float, w: float) -> int:
+    """Largest u in [0, 2^32) with (u * 2^-32) * max_weight <= w (the
+    engine's integer form of the max-weight rejection test)."""
+    lo, hi = 0, 0xFFFFFFFF
+    while lo < hi:
+        mid = lo + (hi - lo + 1) // 2
+        if (mid * (1.0 / 4294967296.0)) * max_weight <= w:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
+
+
+def node2vec(paths: np.ndarray, length: int, seed=None, id_base: int = 0, p: float = 2.0, q: float = 0.5) -> float:
     """Bytes per move of Node2Vec walks with the edge-set neighbour test
-    (walks that stop early are charged the row pair of their last vertex)."""
-    frm, to, k, p = _moves(paths)
+    (walks that stop early are charged the row pair of their last vertex).
+    With the walks' seed, a move is charged the probe only when the engine
+    makes one: its first trial's acceptance draw lies above the lower of the
+    common-neighbour and other-vertex thresholds (below it the move is
+    accepted whatever the probe would say; a move accepted at a later trial
+    is charged as if it had probed)."""
+    frm, to, k, pth = _moves(paths)
     if frm.size == 0:
         return 0.0
     # previous vertex of each move: path entry k-2 (none for the first move)
-    prev = np.full(p[:, :-1].shape, -1, dtype=np.int64)
-    prev[:, 1:] = p[:, :-2]
-    valid = (p[:, :-1] >= 0) & (p[:, 1:] >= 0)
+    prev = np.full(pth[:, :-1].shape, -1, dtype=np.int64)
+    prev[:, 1:] = pth[:, :-2]
+    valid = (pth[:, :-1] >= 0) & (pth[:, 1:] >= 0)
     prev = prev[valid]
     probe = (k >= 2) & (to != prev)
-    total = frm.size * (SECTOR + SECTOR + 4) + int(probe.sum()) * SECTOR + _stops(p, length).size * SECTOR
+    if seed is not None:
+        walker = np.broadcast_to(np.arange(pth.shape[0], dtype=np.int64)[:, None] + id_base, valid.shape)[valid]
+        u = philox_word(int(seed), walker, k, 0, 1)  # trial 0: words 0 (position) and 1 (acceptance)
+        mx = max(1.0, 1.0 / q, 1.0 / p)
+        lo = min(accept_threshold(mx, 1.0), accept_threshold(mx, 1.0 / q))
+        probe &= u > np.uint32(lo)
+    total = frm.size * (SECTOR + SECTOR + 4) + int(probe.sum()) * SECTOR + _stops(pth, length).size * SECTOR
     return total / frm.size
 
 

@@ -287,6 +287,24 @@ __device__ __forceinline__ int n2v_class(const WalkParams &p, int32_t len, int32
     return n2v_neighbor(p.g, prev, prev_row, nbr) ? 2 : 3;
 }
 
+// Node2Vec's max-weight rejection test for acceptance draw u: u <=
+// accept_max[class of nbr].  When the candidate is neither the first move
+// nor a return, its class is 2 or 3 and the neighbour test (a probe of the
+// edge set) only matters for draws between the two classes' thresholds:
+// below both the move is accepted and above both rejected, whichever class
+// it is.  The decision is the one the hook's weight gives
+// (rejection_sampling.h:384-389, node2vec.cpp:182-196) with the probe skipped
+// where it cannot change it.
+__device__ __forceinline__ bool n2v_accept(const WalkParams &p, int32_t len, int32_t prev, int2 prev_row,
+                                           int32_t nbr, uint32_t u) {
+    if (len == 1) return u <= p.accept_max[0];
+    if (nbr == prev) return u <= p.accept_max[1];
+    const uint32_t lo = min(p.accept_max[2], p.accept_max[3]), hi = max(p.accept_max[2], p.accept_max[3]);
+    if (u <= lo) return true;
+    if (u > hi) return false;
+    return u <= p.accept_max[n2v_neighbor(p.g, prev, prev_row, nbr) ? 2 : 3];
+}
+
 // The update hook: length_ == l_, or PPR's real1(termination draw) <= tp.
 template <int U>
 __device__ __forceinline__ bool app_update(const WalkParams &p, uint64_t wid, int32_t len) {

@@ -311,8 +311,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
                 nb = __ldg(g.adj + s[r].crow.x + p0);
                 bool accept;
                 if (WK == kNode2Vec) {
-                    const int k = n2v_class(p, s[r].len, s[r].prev, s[r].prow, nb);
-                    accept = c.next() <= p.accept_max[k];
+                    accept = n2v_accept(p, s[r].len, s[r].prev, s[r].prow, nb, c.next());
                 } else if (WK == kUnitWeight) {
                     accept = c.next() <= p.accept_max[2];
                 } else {
