@@ -160,6 +160,22 @@ int trw_tables_build(trw_graph *g, int32_t sampler, int32_t weight_kind, trw_str
  * (edge_weight_rejection_max_, graph.h:83). */
 int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t out_bytes);
 
+/* Installs a precomputed table (host or device memory, the layout
+ * trw_tables_download produces and the reference's preprocessors write:
+ * b_edge_weight_alias_table.bin, b_edge_weight_prefix_sum.bin,
+ * b_edge_weight_max.bin) as the graph's table for `sampler` built with
+ * `weight_kind` weights, so that static walks with those weights use it
+ * without building one.  Replaces the loading of those files by
+ * Graph::load_csr (graph.cpp:78-94) under -ep / -al / -rj
+ * (creeper_main.h:44-55).  `bytes` must be the table's size (alias: e x 16,
+ * ITS: e x 8, rejection: n x 8).  A table the walks may still be reading is
+ * replaced only after the device has finished them.  The reference's
+ * compute() rebuilds its tables from the edge weights even when the files
+ * were loaded (creeper.h:107-108); a table built by the reference's
+ * preprocessors or by trw_tables_build is bit-identical to that rebuild. */
+int trw_tables_upload(trw_graph *g, int32_t sampler, int32_t weight_kind, const void *table, size_t bytes,
+                      trw_stream_t stream);
+
 /* ---- walks ------------------------------------------------------------ */
 
 /* Replaces compute<F>(graph, walkers, f) (creeper.h:689-831) for the five

@@ -155,6 +155,26 @@ public:
                      e);
     }
 
+    // The precomputed sampling tables the reference loads under -ep, -al and
+    // -rj (graph.cpp:78-94: b_edge_weight_prefix_sum.bin,
+    // b_edge_weight_alias_table.bin, b_edge_weight_max.bin), installed as the
+    // graph's edge-weight tables so that static walks do not build them.
+    void load_tables(const std::string &dir, bool prefix_sum, bool alias_table, bool rejection_max) {
+        auto install = [&](const char *name, int32_t sampler, size_t bytes) {
+            std::vector<char> buf(bytes);
+            std::ifstream f(dir + "/" + name, std::ios::binary);
+            if (!f || !f.read(buf.data(), (std::streamsize)bytes))
+                throw Error(TRW_ERR_INVALID, "cannot read " + dir + "/" + name);
+            check(trw_tables_upload(h_.get(), sampler, TRW_WEIGHTS_EDGE, buf.data(), bytes, nullptr));
+            loaded_ |= 1u << sampler;
+        };
+        if (prefix_sum) install("b_edge_weight_prefix_sum.bin", TRW_SAMPLER_ITS, 8 * (size_t)e_);
+        if (alias_table) install("b_edge_weight_alias_table.bin", TRW_SAMPLER_ALIAS, 16 * (size_t)e_);
+        if (rejection_max) install("b_edge_weight_max.bin", TRW_SAMPLER_REJECTION, 8 * (size_t)n_);
+    }
+    // Whether load_tables installed the edge-weight table of `sampler`.
+    bool table_loaded(int32_t sampler) const { return (loaded_ >> sampler) & 1u; }
+
     int32_t num_vertices() const { return n_; }
     int64_t num_edges() const { return e_; }
     int32_t max_degree() const { return max_degree_; }
@@ -173,6 +193,7 @@ private:
     int32_t n_ = 0;
     int64_t e_ = 0;
     int32_t max_degree_ = 0;
+    uint32_t loaded_ = 0;
 };
 
 // Walker generators (walker_generator.cpp:9-63).  The reference shuffles

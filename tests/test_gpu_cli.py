@@ -68,3 +68,48 @@ def test_cli_matches_oracle(graph_dir, tmp_path, app, args, desc):
     if app == "ppr":
         hub = int(np.argmax(np.diff(og.row)))
         assert np.all(src == hub) and src.size == 3000
+
+
+@pytest.mark.parametrize("flag,sampler,sm", [("-al", "alias", "2"), ("-ep", "its", "1"), ("-rj", "rejection", "3")])
+def test_cli_loads_precomputed_tables(graph_dir, tmp_path, flag, sampler, sm):
+    """-al / -ep / -rj read the reference's table files (written here from the
+    oracle's builders, byte-identical to the reference preprocessors' output)
+    and the static walk uses them instead of building its own; the walks are
+    the oracle's, and no initialization (table build) is logged."""
+    from thunderrw_gb300 import formats
+    d, og = graph_dir
+    tdir = tmp_path / "tables"
+    og.build_tables(sampler, 0)
+    kw = {"alias": dict(alias=og.alias), "its": dict(prefix=og.prefix), "rejection": dict(rmax=og.rej_max)}[sampler]
+    formats.store_csr(str(tdir), og.row, og.adj, weight=og.weight, label=og.label, **kw)
+    steps, paths, lengths, out = _run("deepwalk", ["-f", str(tdir), "-ew", flag, "-em", "1", "-sm", sm, "-l", "11"],
+                                      str(tmp_path / "out"))
+    assert "Loaded tables" in out and "Initialization time" not in out
+    ref = O.walk(og, O.make_desc("deepwalk", "static", sampler, length=11, seed=1), paths[:, 0].copy(), path_cap=11)
+    assert steps == ref["steps"]
+    np.testing.assert_array_equal(paths, ref["paths"])
+
+
+def test_upload_table_round_trip():
+    """A table downloaded from one graph and uploaded into another copy of it
+    gives the same walks as building it there; a wrong size is refused."""
+    torch, E = need_gpu()
+    from thunderrw_gb300 import _native as N
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("chunglu", 1 << 12, 10, seed=5)
+    a = E.Graph(g["row"], g["adj"], g["weight"])
+    b = E.Graph(g["row"], g["adj"], g["weight"])
+    try:
+        a.build_tables("alias", "edge")
+        tab = a.download_table("alias")
+        b.upload_table("alias", tab)
+        assert b.download_table("alias").tobytes() == tab.tobytes()
+        src = G.all_sources(g["row"], seed=2)[:1500]
+        ra = E.compute(a, src, E.DeepWalk(20), seed=3)
+        rb = E.compute(b, src, E.DeepWalk(20), seed=3)
+        assert torch.equal(ra.paths, rb.paths) and ra.steps == rb.steps
+        with pytest.raises(N.TrwError):
+            b.upload_table("alias", tab[:-1])
+    finally:
+        a.close()
+        b.close()

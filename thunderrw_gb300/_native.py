@@ -22,7 +22,7 @@ SAMPLERS = {"uniform": 0, "its": 1, "alias": 2, "rejection": 3, "maxweight_rejec
 ENGINES = {"persistent": 0, "plain": 1}
 WEIGHTS = {"edge": 0, "unit": 1}
 
-EXPORTS = ["trw_graph_create", "trw_graph_destroy", "trw_graph_info", "trw_graph_synchronize", "trw_graph_indexes", "trw_graph_build_indexes", "trw_tables_build", "trw_tables_download",
+EXPORTS = ["trw_graph_create", "trw_graph_destroy", "trw_graph_info", "trw_graph_synchronize", "trw_graph_indexes", "trw_graph_build_indexes", "trw_tables_build", "trw_tables_download", "trw_tables_upload",
            "trw_walk", "trw_ppr_batch", "trw_ppr_batch_sparse", "trw_set_engine_shape", "trw_get_engine_shape",
            "trw_profile_enable", "trw_profile_read", "trw_last_error",
            "trw_device_error", "trw_version"]
@@ -62,6 +62,7 @@ def load(path: str = LIB_PATH):
     L.trw_graph_build_indexes.argtypes = [P, I32, I32, P]
     L.trw_tables_build.argtypes = [P, I32, I32, P]
     L.trw_tables_download.argtypes = [P, I32, P, ctypes.c_size_t]
+    L.trw_tables_upload.argtypes = [P, I32, I32, P, ctypes.c_size_t, P]
     L.trw_walk.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, I32, P, P, P, I32, P]
     L.trw_ppr_batch.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, P, U32, I32, P]
     L.trw_ppr_batch_sparse.argtypes = [P, ctypes.POINTER(WalkDesc), P, I64, I64, P, P, P, I64, P, I32, P]

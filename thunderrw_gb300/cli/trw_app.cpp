@@ -8,8 +8,11 @@
 // defaults and the same summary lines, over include/trw.hpp.
 //
 // Graph flags: -f <dir> (required), -ew, -el (load edge weights / labels),
-// -n <threads> (accepted; the walk runs on the GPU), -vl -vw -ep -al -rj
-// (accepted; sampling tables are built on the GPU, identical to the files).
+// -n <threads> (accepted; the walk runs on the GPU), -vl -vw (accepted),
+// -ep -al -rj (the precomputed edge-weight tables are read and installed, and
+// a static walk with edge weights then uses them instead of building its
+// own; the reference reads them and rebuilds, creeper.h:107-108, which for
+// files written by its preprocessors gives the same tables).
 // App flags (defaults as in each execute()):
 //   deepwalk    -l 80 -em 1 -sm 2                (deepwalk.cpp:32-70)
 //   ppr         -sp 0.2 -nw |V| -em 0 -sm 0      (ppr.cpp:36-88)
@@ -99,7 +102,8 @@ int run(trw::Graph &g, std::vector<trw::WalkerMeta> &walkers, const App &app, tr
              kModes[para.execution_ % 3], kSamplers[para.sample_ % 5], threads, para.length_, walkers.size(),
              (unsigned long long)seed);
     // static_initialization runs before the walk timer (creeper.h:700-739)
-    if (para.execution_ == trw::Static) {
+    if (para.execution_ == trw::Static &&
+        !(App::app != TRW_APP_PPR && g.table_loaded(para.sample_))) {
         const int kind = App::app == TRW_APP_PPR ? TRW_WEIGHTS_UNIT : TRW_WEIGHTS_EDGE;
         const auto t0 = std::chrono::steady_clock::now();
         trw::check(trw_tables_build(g.handle(), para.sample_, kind, nullptr));
@@ -206,6 +210,11 @@ int main(int argc, char **argv) {
         log_info("Graph: |V| = %d, |E| = %lld, max degree = %d, %s, %s", g.num_vertices(),
                  (long long)g.num_edges(), g.max_degree(), fl.has("-ew") ? "edge weighted" : "edge unweighted",
                  fl.has("-el") ? "edge labeled" : "edge unlabeled");
+        if (fl.has("-ep") || fl.has("-al") || fl.has("-rj")) {
+            g.load_tables(dir, fl.has("-ep"), fl.has("-al"), fl.has("-rj"));
+            log_info("Loaded tables:%s%s%s", fl.has("-ep") ? " prefix sums" : "", fl.has("-al") ? " alias" : "",
+                     fl.has("-rj") ? " rejection maxima" : "");
+        }
         const int rc = execute(g, fl, threads);
         if (rc == 0) log_info("Done.");
         return rc;

@@ -889,6 +889,33 @@ int trw_tables_download(const trw_graph *g, int32_t sampler, void *out, size_t o
     return TRW_OK;
 }
 
+int trw_tables_upload(trw_graph *g, int32_t sampler, int32_t weight_kind, const void *table, size_t bytes,
+                      trw_stream_t stream) {
+    if (!g || !table) return fail(TRW_ERR_INVALID, "null argument");
+    if (weight_kind != TRW_WEIGHTS_EDGE && weight_kind != TRW_WEIGHTS_UNIT) return fail(TRW_ERR_INVALID, "bad weight kind");
+    size_t want = 0;
+    if (sampler == TRW_SAMPLER_ALIAS) want = sizeof(AliasSlot) * (size_t)g->e;
+    else if (sampler == TRW_SAMPLER_ITS) want = sizeof(double) * (size_t)g->e;
+    else if (sampler == TRW_SAMPLER_REJECTION) want = sizeof(double) * (size_t)g->n;
+    else return fail(TRW_ERR_INVALID, "sampler %d has no static table", sampler);
+    if (bytes != want) return fail(TRW_ERR_INVALID, "table holds %zu bytes, this graph's needs %zu", bytes, want);
+    std::lock_guard<std::mutex> lock(g->mu);
+    TRW_CUDA(cudaSetDevice(g->device));
+    const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    void **dst = sampler == TRW_SAMPLER_ALIAS ? reinterpret_cast<void **>(&g->alias)
+               : sampler == TRW_SAMPLER_ITS ? reinterpret_cast<void **>(&g->prefix)
+                                            : reinterpret_cast<void **>(&g->rmax);
+    if (*dst) TRW_CUDA(cudaDeviceSynchronize());  // walks on any stream may still read the old table
+    else TRW_CUDA(cudaMalloc(dst, std::max<size_t>(want, 16)));
+    if (want) TRW_CUDA(cudaMemcpyAsync(*dst, table, want, cudaMemcpyDefault, st));
+    if (sampler == TRW_SAMPLER_ALIAS) g->alias_kind = weight_kind;
+    else if (sampler == TRW_SAMPLER_ITS) g->prefix_kind = weight_kind;
+    else g->rmax_kind = weight_kind;
+    TRW_CUDA(cudaEventRecord(g->tables_done, st));
+    TRW_CUDA(cudaStreamSynchronize(st));  // the caller may free or reuse `table` on return
+    return TRW_OK;
+}
+
 int trw_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, int64_t num_walkers, int64_t id_base,
              int32_t *paths, int32_t path_cap, int32_t *lengths, int32_t *counts, uint64_t *steps, int32_t engine,
              trw_stream_t stream) {

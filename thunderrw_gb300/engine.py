@@ -167,6 +167,14 @@ class Graph:
         N.check(_lib().trw_tables_download(self._h, N.SAMPLERS[sampler], out.ctypes.data, out.nbytes))
         return out
 
+    def upload_table(self, sampler: str, table, weights: str = "edge", stream=None):
+        """Installs a precomputed table (trw_tables_upload): an AliasSlot
+        array, ITS prefix sums or rejection maxima, e.g. read from the
+        reference's b_edge_weight_*.bin files."""
+        arr = np.ascontiguousarray(table)
+        N.check(_lib().trw_tables_upload(self._h, N.SAMPLERS[sampler], N.WEIGHTS[weights], arr.ctypes.data,
+                                         arr.nbytes, ctypes.c_void_p(_stream_ptr(stream))))
+
     def set_engine_shape(self, sampler: str, walkers_per_thread: int = 0, ctas_per_sm: int = 0):
         N.check(_lib().trw_set_engine_shape(self._h, N.SAMPLERS[sampler], walkers_per_thread, ctas_per_sm))
 
