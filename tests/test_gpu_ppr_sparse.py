@@ -34,6 +34,53 @@ def _check_against_dense(sp, dense):
         np.testing.assert_array_equal(c[order], dense[q][nz])
 
 
+def _table_bits(wpq, tp, n):
+    """Table size of a query: 2^bits >= 1.25 x its expected visits, at most 2 n."""
+    bits = 10
+    while bits < 30 and (1 << bits) < 1.25 * wpq / tp:
+        bits += 1
+    while bits > 10 and (1 << (bits - 1)) >= 2 * n:
+        bits -= 1
+    return bits
+
+
+def _canonical(vertices, bits):
+    """The emit order of one query's table: linear probing on key v + 1 at
+    slot (v * 0x9E3779B1 mod 2^32) >> (32 - bits), whose set of occupied
+    slots does not depend on the insertion order; runs of occupied slots in
+    slot order with their keys sorted, the run wrapping around the end last."""
+    C = 1 << bits
+    keys = np.zeros(C, dtype=np.int64)
+    for v in np.sort(vertices):
+        h = ((int(v) * 0x9E3779B1) & 0xFFFFFFFF) >> (32 - bits)
+        while keys[h]:
+            h = (h + 1) & (C - 1)
+        keys[h] = int(v) + 1
+    occ = keys != 0
+    head = tail = 0
+    if occ[0] and occ[-1]:
+        head = int(np.argmin(occ))
+        tail = int(np.argmin(occ[::-1]))
+    out, run = [], []
+    for i in range(head, C - tail):
+        if occ[i]:
+            run.append(keys[i])
+        elif run:
+            out += sorted(run)
+            run = []
+    out += sorted(run)
+    out += sorted(list(keys[C - tail:]) + list(keys[:head]))
+    return np.array(out, dtype=np.int64) - 1
+
+
+def _check_canonical(sp, bits):
+    off = sp.offsets.cpu().numpy()
+    vert = sp.vertices.cpu().numpy()
+    for q in range(off.size - 1):
+        v = vert[off[q]:off[q + 1]]
+        np.testing.assert_array_equal(v, _canonical(v, bits), err_msg=f"query {q}")
+
+
 def test_sparse_matches_oracle_and_dense(rmat):
     torch, E = need_gpu()
     from thunderrw_gb300 import generators as G
@@ -54,6 +101,7 @@ def test_sparse_matches_oracle_and_dense(rmat):
         assert torch.equal(outs[0].offsets, outs[1].offsets)
         assert torch.equal(outs[0].vertices[:total], outs[1].vertices[:total])
         assert torch.equal(outs[0].counts[:total], outs[1].counts[:total])
+        _check_canonical(outs[0], _table_bits(700, 0.2, g.n))
         dense, _ = E.ppr_batch(g, qs, 700, tp=0.2, seed=77)
         _check_against_dense(outs[0], dense.cpu().numpy())
         assert torch.equal(outs[0].dense(g.n), dense)
@@ -139,14 +187,16 @@ def test_sparse_host_ranges_match_device(rmat, pinned):
         g.close()
 
 
-def test_sparse_order_with_wrapping_runs():
-    """Dense visits (every query reaches most of a 512-vertex graph) fill the
-    smallest tables to about half, so runs that wrap around the table end
-    are common; the output order must still be the same under both
-    schedules, and the counts the oracle's."""
+@pytest.mark.parametrize("n", [512, 1024, 4096])
+def test_sparse_order_with_wrapping_runs(n):
+    """Dense visits (every query reaches most of the graph) fill tables of
+    2n slots to about half, so long runs and runs that wrap around the table
+    end are common; the output order must be the canonical one under both
+    schedules, and the counts the oracle's.  Tables of 1024 slots take the
+    32-slots-a-warp emit kernel, larger ones the 128-slots-a-warp one."""
     torch, E = need_gpu()
     from thunderrw_gb300 import generators as G
-    g = G.make_graph("er", 512, 48, seed=5, weights=False)
+    g = G.make_graph("er", n, 48, seed=5, weights=False)
     row, adj = g["row"].numpy(), g["adj"].numpy()
     qs = G.random_sources(g["row"], 96, seed=6).numpy()
     og = O.Graph(row, adj)
@@ -158,7 +208,10 @@ def test_sparse_order_with_wrapping_runs():
         b = E.ppr_batch_sparse(gr, qs, 4000, tp=0.2, seed=9, engine="plain")
         _check_against_dense(a, ref["counts"])
         total = int(a.offsets[-1].item())
-        assert total > 96 * 256  # about half of each 1024-slot table is occupied
+        bits = _table_bits(4000, 0.2, n)
+        if n == 512:
+            assert bits == 10 and total > 96 * 256  # about half of each 1024-slot table is occupied
+        _check_canonical(a, bits)
         assert torch.equal(a.offsets, b.offsets)
         assert torch.equal(a.vertices[:total], b.vertices[:total])
         assert torch.equal(a.counts[:total], b.counts[:total])
@@ -185,6 +238,9 @@ def test_sparse_large_tables_split_over_ctas(queries, wpq):
         b = E.ppr_batch_sparse(gr, qs, wpq, tp=0.2, seed=19, engine="plain")
         _check_against_dense(a, ref["counts"])
         total = int(a.offsets[-1].item())
+        bits = _table_bits(wpq, 0.2, 1 << 17)
+        assert bits > 16
+        _check_canonical(a, bits)
         assert torch.equal(a.offsets, b.offsets)
         assert torch.equal(a.vertices[:total], b.vertices[:total])
         assert torch.equal(a.counts[:total], b.counts[:total])

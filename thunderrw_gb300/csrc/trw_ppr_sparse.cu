@@ -27,8 +27,8 @@
 namespace trw {
 namespace {
 
-constexpr int kScanThreads = 1024;
-constexpr int kEmitThreads = 512;
+constexpr int kScanThreads = 256;
+constexpr int kEmitThreads = 256;
 
 template <typename T>
 __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T &total) {
@@ -137,28 +137,37 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 //   pos = (occupied slots before it) - (slots of the wrapping run at the table
 //         start) - (its distance back to the run start) + (rank of its key
 //         among the run's keys)
-// A warp walks its segment 32 slots at a time with coalesced loads and keeps
-// the previous, current and next blocks of keys in registers (two more blocks
-// in flight): the run of a slot is found from the three occupancy ballots and
-// its key ranked against the run through shuffles.  Runs reaching beyond that
-// 96-slot window, and the wrapping run, are read from global memory, which
-// stays intact until the final zeroing.
+// A warp takes 128 slots of its segment per iteration (segments are
+// multiples of 128 slots: tables have at least 2^10 slots, chunks 2^16 at
+// most, 8 warps a CTA), lane l owning slots l, l + 32, l + 64 and l + 96.
+// Keys arrive with 16-byte loads into a per-warp ring of four 128-slot blocks
+// in shared memory (the previous, current and next block, and the one after
+// being filled); four ballots per block give its 128-bit occupancy, from
+// which every slot finds the empty slots before and after its run with
+// clz/ffs over the 384-slot window, and it ranks its key by reading the run
+// from the ring.  Runs reaching beyond the window and the run that wraps
+// around the table end are read from global memory, which stays intact until
+// the zeroing.
+constexpr int32_t kBlk4 = 128;
+constexpr int32_t kRing = 4 * kBlk4;
+
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, const int64_t *offsets,
-                                                            const int32_t *seg_prefix, int32_t *vout, int32_t *cout,
-                                                            int64_t capacity, int *error) {
+                                                             const int32_t *seg_prefix, int32_t *vout, int32_t *cout,
+                                                             int64_t capacity, int *error) {
     __shared__ uint32_t wrap[2];
+    __shared__ __align__(16) int32_t ring_all[kEmitWarps][kRing];
     const uint32_t S = chunks_for(bits);
     const int64_t q = blockIdx.x / S;
     const uint32_t chunk = blockIdx.x % S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nslots = 1u << bits;
     int32_t *keys = tables + (q << (bits + 1));
-    int32_t *cnts = keys + nslots;
+    const int32_t *cnts = keys + nslots;
+    const int4 *k4 = reinterpret_cast<const int4 *>(keys);
     const int64_t end = offsets[q + 1];
     const bool write = end <= capacity;
     if (threadIdx.x == 0) {
         if (!write && chunk == 0) atomicOr(error, kErrCapacity);
-        // the wrapping run: `head` slots from slot 0 and `tail` slots before the end
         uint32_t head = 0, tail = 0;
         if (__ldg(keys) != 0 && __ldg(keys + nslots - 1) != 0) {
             while (head < nslots && __ldg(keys + head) != 0) ++head;
@@ -174,92 +183,124 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     __syncthreads();
     const uint32_t head = wrap[0], tail = wrap[1], cyc = head + tail;
     int64_t prefix = offsets[q] + seg_prefix[(int64_t)blockIdx.x * kEmitWarps + warp];
-
-    const uint32_t seg = nslots / S / kEmitWarps;  // >= 64: tables have >= 1024 slots, chunks 2^16
-    const uint32_t lo = chunk * (nslots / S) + warp * seg, nblk = seg / 32;
-    const uint32_t x0 = lo + lane;
-    auto key_at = [&](uint32_t y) { return y < nslots ? __ldg(keys + y) : 0; };
-    auto cnt_at = [&](uint32_t y) { return y < nslots ? __ldg(cnts + y) : 0; };
-    int32_t kp = lo ? __ldg(keys + lo - 32 + lane) : 0;
-    int32_t kc = key_at(x0), cc = cnt_at(x0);
-    int32_t kn = key_at(x0 + 32), cn = cnt_at(x0 + 32);
-    int32_t k2 = key_at(x0 + 64), c2 = cnt_at(x0 + 64);
-    unsigned op = __ballot_sync(0xffffffffu, kp != 0);
-    const unsigned lt = lanemask_lt(), le = lt | (1u << lane);
-    for (uint32_t b = 0; b < nblk; ++b) {
-        const uint32_t x = x0 + b * 32;
-        const int32_t k3 = key_at(x + 96), c3 = cnt_at(x + 96);
-        const unsigned oc = __ballot_sync(0xffffffffu, kc != 0), on = __ballot_sync(0xffffffffu, kn != 0);
-        const int64_t before = prefix + __popc(oc & lt);
-        prefix += __popc(oc);
-        const bool in_wrap = kc != 0 && (x < head || x >= nslots - tail);
-        // window positions: 0-31 previous block, 32-63 this block, 64-95 next block
-        int s = -1, e = -1;
-        if (kc != 0 && !in_wrap) {
-            const unsigned zb = ~oc & lt, za = ~oc & ~le;
-            if (zb) s = 64 - __clz(zb);
-            else if (~op) s = 32 - __clz(~op);
-            if (za) e = 31 + __ffs(za);
-            else if (~on) e = 63 + __ffs(~on);
-        }
-        const bool fast = s >= 0 && e >= 0;
-        const int len = fast ? e - s : 0;
-        const int maxlen = __reduce_max_sync(0xffffffffu, len);
-        uint32_t rank = 0;
-        if (__all_sync(0xffffffffu, !fast || (s >= 32 && e <= 64))) {
-            // every run of this block lies inside it: rank within this block's keys
-            for (int d = 0; d < maxlen; ++d) {
-                const int j = s + d;
-                const int32_t k = __shfl_sync(0xffffffffu, kc, j & 31);
-                if (d < len && j != 32 + lane) rank += k < kc;
-            }
-        } else {
-            for (int d = 0; d < maxlen; ++d) {
-                const int j = s + d;
-                const int src = j & 31;
-                const int32_t a = __shfl_sync(0xffffffffu, kp, src);
-                const int32_t m = __shfl_sync(0xffffffffu, kc, src);
-                const int32_t n = __shfl_sync(0xffffffffu, kn, src);
-                const int32_t k = j < 32 ? a : j < 64 ? m : n;
-                if (d < len && j != 32 + lane) rank += k < kc;
-            }
-        }
-        if (write && kc != 0) {
-            int64_t pos;
-            if (fast) {
-                pos = before - head - (32 + lane - s) + rank;
-            } else if (in_wrap) {
-                rank = 0;
-                for (uint32_t i = 0; i < cyc; ++i) {
-                    const uint32_t y = i < tail ? nslots - tail + i : i - tail;
-                    rank += __ldg(keys + y) < kc;
+    const uint32_t seg = nslots / S / kEmitWarps;  // a multiple of kBlk4 here
+    const uint32_t lo = chunk * (nslots / S) + warp * seg;
+    const int32_t nblk = (int32_t)(seg / kBlk4);
+    int32_t *ring = ring_all[warp];
+    // block m (slots lo + 128 m ...) sits at ring[((m + 1) * 128) mod 512 ...]
+    auto load_blk = [&](int32_t m) {
+        const int64_t y0 = (int64_t)lo + (int64_t)m * kBlk4;
+        return y0 >= 0 && y0 < (int64_t)nslots ? __ldg(k4 + (y0 >> 2) + lane) : make_int4(0, 0, 0, 0);
+    };
+    auto ring_of = [&](int32_t m) { return ring + (((m + 1) * kBlk4) & (kRing - 1)); };
+    auto ballots = [&](int32_t m, uint32_t(&o)[4]) {
+        const int32_t *r = ring_of(m);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) o[j] = __ballot_sync(0xffffffffu, r[32 * j + lane] != 0);
+    };
+    auto load_cnts = [&](int32_t m, int32_t(&c)[4]) {
+        const uint32_t y0 = lo + (uint32_t)m * kBlk4 + lane;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) c[j] = m < nblk ? __ldg(cnts + y0 + 32 * j) : 0;
+    };
+    reinterpret_cast<int4 *>(ring_of(-1))[lane] = load_blk(-1);
+    reinterpret_cast<int4 *>(ring_of(0))[lane] = load_blk(0);
+    reinterpret_cast<int4 *>(ring_of(1))[lane] = load_blk(1);
+    int4 kf = load_blk(2);
+    int32_t cc[4], cn[4];
+    load_cnts(0, cc);
+    __syncwarp();
+    uint32_t w[12];  // occupancy of the window: blocks b - 1, b, b + 1, 32 slots a word
+    {
+        uint32_t o[4];
+        ballots(-1, o);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) w[j] = o[j];
+        ballots(0, o);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) w[4 + j] = o[j];
+        ballots(1, o);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) w[8 + j] = o[j];
+    }
+    const unsigned lt = lanemask_lt(), gt = ~(lt | (1u << lane));
+    for (int32_t b = 0; b < nblk; ++b) {
+        reinterpret_cast<int4 *>(ring_of(b + 2))[lane] = kf;  // over block b - 2, read before the last __syncwarp
+        kf = load_blk(b + 3);
+        load_cnts(b + 1, cn);
+        const int32_t *rc = ring_of(b);  // window position i (block b - 1 + i / 128) is ring[(b * 128 + i) mod 512]
+        int64_t before = prefix;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int32_t k = rc[32 * j + lane];
+            const int32_t p = kBlk4 + 32 * j + lane;  // this slot's window position
+            const uint32_t xs = lo + (uint32_t)b * kBlk4 + 32 * j + lane;
+            if (write && k != 0) {
+                int64_t pos;
+                if (cyc && (xs < head || xs + tail >= nslots)) {  // the wrap-around run: last, keys sorted
+                    uint32_t rank = 0;
+                    for (uint32_t i = 0; i < cyc; ++i) {
+                        const uint32_t y = i < tail ? nslots - tail + i : i - tail;
+                        rank += __ldg(keys + y) < k;
+                    }
+                    pos = end - cyc + rank;
+                } else {
+                    // the empty window positions before (s) and after (e) the run
+                    int32_t s = -1, e = 3 * kBlk4;
+                    uint32_t z = ~w[4 + j] & lt;
+                    if (z) {
+                        s = 32 * (4 + j) + 31 - __clz(z);
+                    } else {
+#pragma unroll
+                        for (int i = 3 + j; i >= 0; --i)
+                            if (~w[i]) { s = 32 * i + 31 - __clz(~w[i]); break; }
+                    }
+                    z = ~w[4 + j] & gt;
+                    if (z) {
+                        e = 32 * (4 + j) + __ffs(z) - 1;
+                    } else {
+#pragma unroll
+                        for (int i = 5 + j; i < 12; ++i)
+                            if (~w[i]) { e = 32 * i + __ffs(~w[i]) - 1; break; }
+                    }
+                    uint32_t rank = 0, back;
+                    if (s >= 0 && e < 3 * kBlk4) {
+                        back = (uint32_t)(p - s - 1);
+                        for (int32_t i = s + 1; i < e; ++i)
+                            rank += ring[(b * kBlk4 + i) & (kRing - 1)] < k;  // k itself does not count
+                    } else {  // the run reaches beyond the window
+                        back = 0;
+                        while (xs > back && __ldg(keys + xs - back - 1) != 0) ++back;
+                        for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + xs - d) < k;
+                        for (uint32_t y = xs + 1; y < nslots; ++y) {
+                            const int32_t v = __ldg(keys + y);
+                            if (v == 0) break;
+                            rank += v < k;
+                        }
+                    }
+                    pos = before + __popc(w[4 + j] & lt) - head - back + rank;
                 }
-                pos = end - cyc + rank;
-            } else {
-                uint32_t back = 0;
-                while (x > back && __ldg(keys + x - back - 1) != 0) ++back;
-                rank = 0;
-                for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + x - d) < kc;
-                for (uint32_t y = x + 1; y < nslots; ++y) {
-                    const int32_t k = __ldg(keys + y);
-                    if (k == 0) break;
-                    rank += k < kc;
-                }
-                pos = before - head - back + rank;
+                vout[pos] = k - 1;
+                cout[pos] = cc[j] + 1;  // the table counts visits after the first
             }
-            vout[pos] = kc - 1;
-            cout[pos] = cc + 1;  // the table counts visits after the first
+            before += __popc(w[4 + j]);
         }
-        kp = kc; op = oc;
-        kc = kn; cc = cn;
-        kn = k2; cn = c2;
-        k2 = k3; c2 = c3;
+        prefix = before;
+        __syncwarp();
+        uint32_t o[4];
+        ballots(b + 2, o);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = w[j + 4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            w[8 + j] = o[j];
+            cc[j] = cn[j];
+        }
     }
     if (S > 1) return;  // chunked tables are zeroed after the kernel: other CTAs may still read this chunk
     __syncthreads();
-    // zero the table for the next batch (coalesced 16-byte stores)
-    int4 *z = reinterpret_cast<int4 *>(keys);
-    for (uint32_t i = threadIdx.x; i < nslots / 2; i += blockDim.x) z[i] = make_int4(0, 0, 0, 0);
+    int4 *zr = reinterpret_cast<int4 *>(keys);
+    for (uint32_t i = threadIdx.x; i < nslots / 2; i += blockDim.x) zr[i] = make_int4(0, 0, 0, 0);
 }
 
 __global__ void sum_steps_kernel(const unsigned long long *parts, int n, unsigned long long *out) {
