@@ -55,14 +55,15 @@ BYTES_PER_STEP = {
 # workload's walk kernel, from one ncu capture of that kernel: PPR on the
 # full N = 2^22 graph with 256 queries (1.386 GB over 12.80 M steps; the full
 # batch's tables do not change the per-step traffic of the walk: only the
-# in-flight queries' tables are written), DeepWalk on its full graph, Node2Vec
-# and MetaPath on R-MAT 2^22 instances of their graphs.  Scaled by the steps
-# of one full launch.
+# in-flight queries' tables are written), DeepWalk and Node2Vec on their full
+# graphs (Node2Vec with the adjacency entries that carry row pairs), MetaPath
+# on an R-MAT 2^22 instance of its graph.  Scaled by the steps of one full
+# launch.
 TRAFFIC_BYTES_PER_STEP = {
     "ppr": 108.25,
     "ppr_dense": 89.13,
     "deepwalk": 16.47,
-    "node2vec": 198.29,
+    "node2vec": 207.78,
     "metapath": 155.1,
 }
 
@@ -631,7 +632,7 @@ def measure(name, args, over, dev, rank, world, steps, warmup, headline):
         sample = paths[:65536].cpu().numpy()
         if name == "node2vec":  # probes only where the kernel makes them (its draws, from the seed)
             bps = bytes_model.node2vec(sample, wl["length"], seed=replicas.replica_seed(2000 + steps - 1, rank),
-                                       p=wl["p"], q=wl["q"])
+                                       p=wl["p"], q=wl["q"], fat=graph.fat_adjacency() == 1)
         elif graph.indexes()[1] == 1:  # MetaPath answered from the label index
             bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"])
         else:

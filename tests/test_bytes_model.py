@@ -115,3 +115,10 @@ def test_node2vec_model_charges_probes_only_in_the_band():
     full = B.node2vec(r["paths"], 20)
     lazy = B.node2vec(r["paths"], 20, seed=9, p=2.0, q=0.5)
     assert 68.0 < lazy < full
+    # with row pairs in the adjacency entries: one sector less per move, but
+    # each walker's source row pair
+    fat = B.node2vec(r["paths"], 20, seed=9, p=2.0, q=0.5, fat=True)
+    moves = int(((r["paths"][:, :-1] >= 0) & (r["paths"][:, 1:] >= 0)).sum())
+    first = int((r["paths"][:, 1] >= 0).sum())
+    stops = B._stops(r["paths"], 20).size
+    assert fat * moves == pytest.approx(lazy * moves - 32 * moves + 32 * first - 32 * stops)

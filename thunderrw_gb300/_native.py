@@ -22,7 +22,7 @@ SAMPLERS = {"uniform": 0, "its": 1, "alias": 2, "rejection": 3, "maxweight_rejec
 ENGINES = {"persistent": 0, "plain": 1}
 WEIGHTS = {"edge": 0, "unit": 1}
 
-EXPORTS = ["trw_graph_create", "trw_graph_destroy", "trw_graph_info", "trw_graph_synchronize", "trw_graph_indexes", "trw_graph_build_indexes", "trw_tables_build", "trw_tables_download", "trw_tables_upload",
+EXPORTS = ["trw_graph_create", "trw_graph_destroy", "trw_graph_info", "trw_graph_synchronize", "trw_graph_indexes", "trw_graph_layout", "trw_graph_build_indexes", "trw_tables_build", "trw_tables_download", "trw_tables_upload",
            "trw_walk", "trw_ppr_batch", "trw_ppr_batch_sparse", "trw_set_engine_shape", "trw_get_engine_shape",
            "trw_profile_enable", "trw_profile_read", "trw_last_error",
            "trw_device_error", "trw_version"]
@@ -59,6 +59,7 @@ def load(path: str = LIB_PATH):
     L.trw_graph_info.argtypes = [P, P, P, P]
     L.trw_graph_synchronize.argtypes = [P]
     L.trw_graph_indexes.argtypes = [P, P, P]
+    L.trw_graph_layout.argtypes = [P, P]
     L.trw_graph_build_indexes.argtypes = [P, I32, I32, P]
     L.trw_tables_build.argtypes = [P, I32, I32, P]
     L.trw_tables_download.argtypes = [P, I32, P, ctypes.c_size_t]

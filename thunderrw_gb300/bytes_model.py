@@ -89,14 +89,17 @@ def accept_threshold(max_weight: float, w: float) -> int:
     return lo
 
 
-def node2vec(paths: np.ndarray, length: int, seed=None, id_base: int = 0, p: float = 2.0, q: float = 0.5) -> float:
+def node2vec(paths: np.ndarray, length: int, seed=None, id_base: int = 0, p: float = 2.0, q: float = 0.5,
+             fat: bool = False) -> float:
     """Bytes per move of Node2Vec walks with the edge-set neighbour test
     (walks that stop early are charged the row pair of their last vertex).
     With the walks' seed, a move is charged the probe only when the engine
     makes one: its first trial's acceptance draw lies above the lower of the
     common-neighbour and other-vertex thresholds (below it the move is
     accepted whatever the probe would say; a move accepted at a later trial
-    is charged as if it had probed)."""
+    is charged as if it had probed).  ``fat``: the adjacency entries carry
+    the neighbours' row pairs, so a move reads its entry's sector and no row
+    pair; only a walker's source row pair is read (at its admission)."""
     frm, to, k, pth = _moves(paths)
     if frm.size == 0:
         return 0.0
@@ -112,7 +115,10 @@ def node2vec(paths: np.ndarray, length: int, seed=None, id_base: int = 0, p: flo
         mx = max(1.0, 1.0 / q, 1.0 / p)
         lo = min(accept_threshold(mx, 1.0), accept_threshold(mx, 1.0 / q))
         probe &= u > np.uint32(lo)
-    total = frm.size * (SECTOR + SECTOR + 4) + int(probe.sum()) * SECTOR + _stops(pth, length).size * SECTOR
+    if fat:
+        total = frm.size * (SECTOR + 4) + int((k == 1).sum()) * SECTOR + int(probe.sum()) * SECTOR
+    else:
+        total = frm.size * (SECTOR + SECTOR + 4) + int(probe.sum()) * SECTOR + _stops(pth, length).size * SECTOR
     return total / frm.size
 
 

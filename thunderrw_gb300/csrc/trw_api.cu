@@ -7,6 +7,7 @@
 #include <climits>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -128,6 +129,12 @@ struct trw_graph {
     int positive_rows = 0;
     int32_t edge_symmetric = 0;
     int edge_state = 0;
+    // the adjacency with row pairs (DevGraph::fat), built by the first
+    // uniform or max-weight rejection thread-engine walk on a graph whose row
+    // pairs outgrow half the L2; fat_state 0 = not yet, 1 = built, -1 = not
+    // built (the walks then read the row pairs)
+    int4 *fat = nullptr;
+    int fat_state = 0;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
     unsigned long long *state = nullptr;
     int *error = nullptr;
@@ -168,7 +175,7 @@ void destroy_graph(trw_graph *g) {
     if (!g) return;
     cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state); cudaFree(g->edges);
-    cudaFree(g->long_rows); cudaFree(g->lab_nbr); cudaFree(g->lab_off);
+    cudaFree(g->long_rows); cudaFree(g->lab_nbr); cudaFree(g->lab_off); cudaFree(g->fat);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
@@ -195,6 +202,7 @@ DevGraph dev_view(const trw_graph *g) {
     d.lab_nbr = g->lab_state == 1 ? g->lab_nbr : nullptr;
     d.lab_off = g->lab_state == 1 ? g->lab_off : nullptr;
     d.lab_k = g->lab_state == 1 ? g->lab_k : 0;
+    d.fat = g->fat_state == 1 ? g->fat : nullptr;
     return d;
 }
 
@@ -232,6 +240,35 @@ int build_label_index(trw_graph *g, cudaStream_t st) {
     TRW_CUDA(cudaStreamSynchronize(st));
     g->lab_k = K;
     g->lab_state = 1;
+    return TRW_OK;
+}
+
+// The adjacency with the neighbours' row pairs folded in (16 bytes per
+// edge): a move reads one entry instead of the row pair and then the entry.
+// Worth its memory only where the row pairs are DRAM reads: when they take
+// more than half the L2 (R-MAT 2^24: 128 MB of row pairs, Node2Vec's DRAM
+// traffic per step falls; R-MAT 2^22: 32 MB, L2 hits, no change measured).
+// If the device has no room for it the walks keep the two loads.
+int build_fat_adjacency(trw_graph *g, cudaStream_t st) {
+    if (g->fat_state != 0 || g->e <= 0) return TRW_OK;
+    // TRW_FAT_ADJACENCY=0 / 1 turns the rule off / on for every graph
+    const char *force = getenv("TRW_FAT_ADJACENCY");
+    int l2 = 0;
+    TRW_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, g->device));
+    const bool want = force && *force ? *force == '1' : sizeof(int2) * (size_t)g->n > (size_t)l2 / 2;
+    if (!want) { g->fat_state = -1; return TRW_OK; }
+    const size_t bytes = sizeof(int4) * (size_t)g->e;
+    size_t free_b = 0, total_b = 0;
+    TRW_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes + (size_t(1) << 30) > free_b || cudaMalloc(&g->fat, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        g->fat = nullptr;
+        g->fat_state = -1;
+        return TRW_OK;
+    }
+    TRW_CUDA(launch_build_fat(dev_view(g), g->fat, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    g->fat_state = 1;
     return TRW_OK;
 }
 
@@ -508,6 +545,10 @@ int prepare_plan(trw_graph *g, const trw_walk_desc *desc, Plan &pl, cudaStream_t
 
     if (desc->app == TRW_APP_NODE2VEC && g->edge_state == 0) {
         rc = build_edge_set(g, st);
+        if (rc) return rc;
+    }
+    if (!pl.warp_family && (pl.sampler == kUniform || pl.sampler == kMaxRejection) && g->fat_state == 0) {
+        rc = build_fat_adjacency(g, st);
         if (rc) return rc;
     }
     if (desc->app == TRW_APP_METAPATH && pl.warp_family && pl.sampler == kITS) {
@@ -838,6 +879,12 @@ int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *labe
     if (!g) return fail(TRW_ERR_INVALID, "null graph");
     if (edge_set_state) *edge_set_state = g->edge_state;
     if (label_index_state) *label_index_state = g->lab_state;
+    return TRW_OK;
+}
+
+int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state) {
+    if (!g || !fat_adjacency_state) return fail(TRW_ERR_INVALID, "null argument");
+    *fat_adjacency_state = g->fat_state;
     return TRW_OK;
 }
 

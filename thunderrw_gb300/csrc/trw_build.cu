@@ -420,6 +420,15 @@ __global__ void build_edge_set_kernel(DevGraph g, unsigned long long *set, int32
     }
 }
 
+// The uniform moves' adjacency with the neighbours' row pairs (DevGraph::fat).
+__global__ void build_fat_kernel(DevGraph g, int4 *fat) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.e) return;
+    const int32_t v = __ldg(g.adj + i);
+    const int2 r = __ldg(g.rows + v);
+    fat[i] = make_int4(v, r.x, r.y, 0);
+}
+
 // Clears *symmetric if some edge's reverse is missing.
 __global__ void edge_symmetry_kernel(DevGraph g, int *symmetric) {
     const int64_t first = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kEdgeRun;
@@ -495,6 +504,12 @@ cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, in
     gs.edges = set;
     gs.edge_bits = bits;
     edge_symmetry_kernel<<<grid, 256, 0, st>>>(gs, symmetric);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_fat(const DevGraph &g, int4 *fat, cudaStream_t st) {
+    if (g.e <= 0) return cudaSuccess;
+    build_fat_kernel<<<blocks_for(g.e), 256, 0, st>>>(g, fat);
     return cudaGetLastError();
 }
 

@@ -108,6 +108,12 @@ struct DevGraph {
     const int32_t *lab_nbr;
     const int32_t *lab_off;
     int32_t lab_k;
+    // The adjacency with the row pairs folded in, for uniform and max-weight
+    // rejection moves on graphs whose row pairs do not stay in L2: entry i
+    // holds {adj[i], rows[adj[i]].x, rows[adj[i]].y, 0}, so one 16-byte load
+    // gives the next vertex and the row it will sample from (null if not
+    // built).
+    const int4 *fat;
     int32_t n;
     int64_t e;
 };

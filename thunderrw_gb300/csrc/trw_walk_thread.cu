@@ -38,6 +38,9 @@ __device__ __forceinline__ void finish(const WalkParams &p, Slot &s) {
     s.widx = -1;
 }
 
+// kFat: the walk moves through DevGraph::fat when it is built, so the slot
+// carries the current vertex's row pair (read here for the source).
+template <bool kFat>
 __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx) {
     int64_t q = 0;
     int32_t src;
@@ -56,6 +59,7 @@ __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx)
         return;
     }
     s.cur = src;
+    if (kFat && p.g.fat) s.crow = __ldg(p.g.rows + src);
 }
 
 __device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
@@ -165,7 +169,12 @@ template <int S, int U, int WK, int R, bool kSparse>
 __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uint64_t &steps,
                                           PendingInsert (&pend)[R][kInsertDepth]) {
     const DevGraph &g = p.g;
+    // uniform and max-weight rejection moves through the adjacency with row
+    // pairs: the slot already holds the current row, and the entry a move
+    // takes brings the next one with its vertex
+    const bool fat = (S == kUniform || S == kMaxRejection) && g.fat != nullptr;
     int32_t nxt[R];
+    int2 nrow[R];
     bool moved[R];
     uint4 rnd[R];
 #pragma unroll
@@ -173,7 +182,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         moved[r] = false;
         nxt[r] = 0;
         // the label index holds CSR positions itself: no row pair to read
-        if (S != kLabelIndex && s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
+        if (S != kLabelIndex && !fat && s[r].widx >= 0) s[r].crow = __ldg(g.rows + s[r].cur);
     }
     if (kSparse) {  // while the row pairs are in flight
 #pragma unroll
@@ -192,7 +201,16 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         for (int r = 0; r < R; ++r) {
             if (s[r].widx < 0) continue;
             const int32_t deg = s[r].crow.y - s[r].crow.x;
-            if (deg > 0) { nxt[r] = __ldg(g.adj + s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg)); moved[r] = true; }
+            if (deg <= 0) continue;
+            const int32_t at = s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg);
+            if (fat) {
+                const int4 f = __ldg(g.fat + at);
+                nxt[r] = f.x;
+                nrow[r] = make_int2(f.y, f.z);
+            } else {
+                nxt[r] = __ldg(g.adj + at);
+            }
+            moved[r] = true;
         }
     } else if (S == kAlias) {
         // static_alias_interleaving_move (alias_sampling.h:221-258)
@@ -306,9 +324,16 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
             DrawCursor c(p.seed, (uint64_t)(p.id_base + s[r].widx), (uint32_t)s[r].len, rnd[r]);
             uint32_t trials = 0;
             int32_t nb;
+            int2 nbrow = make_int2(0, 0);
             for (;;) {
                 const int32_t p0 = (int32_t)(c.next() % (uint32_t)deg);
-                nb = __ldg(g.adj + s[r].crow.x + p0);
+                if (fat) {
+                    const int4 f = __ldg(g.fat + s[r].crow.x + p0);
+                    nb = f.x;
+                    nbrow = make_int2(f.y, f.z);
+                } else {
+                    nb = __ldg(g.adj + s[r].crow.x + p0);
+                }
                 bool accept;
                 if (WK == kNode2Vec) {
                     accept = n2v_accept(p, s[r].len, s[r].prev, s[r].prow, nb, c.next());
@@ -323,6 +348,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
             }
             if (trials >= kMaxTrials) { atomicOr(p.error, kErrTrials); continue; }
             nxt[r] = nb;
+            nrow[r] = nbrow;
             moved[r] = true;
         }
     }
@@ -336,6 +362,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         s[r].prev = s[r].cur;
         if (S != kLabelIndex) s[r].prow = s[r].crow;  // (the label index reads no row pair)
         s[r].cur = nxt[r];
+        if (fat) s[r].crow = nrow[r];
         if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
         s[r].len += 1;
         steps += 1;
@@ -387,7 +414,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
                 const unsigned avail = (unsigned)min(res_end - res_next, 32ull);
                 const unsigned rank = __popc(need & lanemask_lt());
                 const bool mine = ((need >> lane) & 1u) && rank < avail;
-                if (mine) admit(p, s[r], (int64_t)(res_next + rank));
+                if (mine) admit<S == kUniform || S == kMaxRejection>(p, s[r], (int64_t)(res_next + rank));
                 res_next += min((unsigned)__popc(need), avail);
                 need &= ~__ballot_sync(kFull, mine);
             }
@@ -415,7 +442,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
         Slot s[1];
         PendingInsert pend[1][kInsertDepth];
             for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
-        admit(p, s[0], idx);
+        admit<S == kUniform || S == kMaxRejection>(p, s[0], idx);
         while (s[0].widx >= 0) step_ring<S, U, WK, 1, kSparse>(p, s, steps, pend);
         if (kSparse)
             for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[0][k], true);
@@ -468,7 +495,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_multi(const MultiBatch mb, 
             if (mine) {
                 req = r_req;
                 wsteps = 0;
-                admit(mb.reqs[req], s[0], r_next + rank);
+                admit<S == kUniform || S == kMaxRejection>(mb.reqs[req], s[0], r_next + rank);
                 dead = s[0].widx < 0;  // an invalid source finishes at once
             }
             if (dead) {
