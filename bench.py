@@ -632,9 +632,10 @@ def measure(name, args, over, dev, rank, world, steps, warmup, headline):
         sample = paths[:65536].cpu().numpy()
         if name == "node2vec":  # probes only where the kernel makes them (its draws, from the seed)
             bps = bytes_model.node2vec(sample, wl["length"], seed=replicas.replica_seed(2000 + steps - 1, rank),
-                                       p=wl["p"], q=wl["q"], fat=graph.fat_adjacency() == 1)
+                                       p=wl["p"], q=wl["q"], fat=graph.layout()[0] == 1)
         elif graph.indexes()[1] == 1:  # MetaPath answered from the label index
-            bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"])
+            bps = bytes_model.metapath_index(sample, inp["row"].cpu().numpy(), wl["length"],
+                                             fat=graph.layout()[1] == 1)
         else:
             bps = bytes_model.metapath(sample, inp["row"].cpu().numpy(), wl["length"])
     achieved = steps_per_batch * bps / kmean / 1e9

@@ -137,15 +137,20 @@ int trw_graph_synchronize(trw_graph *g);
  * same either way. */
 int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *label_index_state);
 
-/* The adjacency layout the uniform and max-weight rejection walks use (no
- * counterpart in the reference): 1 = the 16-byte entries that carry each
- * neighbour's offset pair (built by the first such walk when the graph's
- * offset pairs, 8 bytes per vertex, exceed half the device's L2; a move then
- * reads one entry instead of the pair and then the entry), 0 = not decided
- * yet, -1 = the plain adjacency (small graph or no room).  The environment
- * variable TRW_FAT_ADJACENCY=1 / 0, read when the decision is made, forces
- * one or the other.  Results are the same either way. */
-int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state);
+/* The layouts the walks read (no counterpart in the reference; results are
+ * the same with either).  fat_adjacency_state, for uniform and max-weight
+ * rejection walks: 1 = 16-byte adjacency entries that carry each neighbour's
+ * offset pair (built by the first such walk when the offset pairs, 8 bytes
+ * per vertex, exceed half the device's L2; a move then reads one entry
+ * instead of the pair and then the entry), 0 = not decided yet, -1 = the
+ * plain adjacency (small graph or no room).  fat_label_index_state, for
+ * MetaPath walks on the label index whose schema names each label at most
+ * once: 1 = 16-byte label-index entries that carry the next step's block of
+ * positions, built by trw_walk for the last such schema (when the label
+ * offsets, 4 (K + 1) bytes per vertex, exceed half the L2), 0 / -1 as
+ * above.  The environment variable TRW_FAT_ADJACENCY=1 / 0, read when a
+ * decision is made, forces both one way. */
+int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state, int32_t *fat_label_index_state);
 
 /* Builds those lookup structures now instead of in the first walk that needs
  * them, e.g. before a serving loop starts so that no request pays for a

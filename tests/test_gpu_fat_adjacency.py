@@ -82,3 +82,41 @@ def test_ppr_uniform(mode, fat_env, rmat):
         np.testing.assert_array_equal(r.lengths.cpu().numpy(), refp["lengths"])
     finally:
         g.close()
+
+
+def _labelled():
+    from thunderrw_gb300 import generators as G
+    g = G.make_graph("rmat", 1 << 12, 24, seed=61, labels=5)
+    return g["row"].numpy(), g["adj"].numpy(), g["label"].numpy()
+
+
+@pytest.mark.parametrize("mode", ["1", "0"])
+def test_metapath_label_index_entries(mode, fat_env):
+    """Schemas that name each label once read the label-index entries that
+    carry the next step's block (forced on here); a schema with a repeated
+    label, one with a label no edge has, and switching schemas on one graph
+    (the entries are rebuilt) all give the oracle's walks."""
+    torch, E = need_gpu()
+    fat_env(mode)
+    row, adj, lab = _labelled()
+    w = np.ones(adj.size)
+    src = np.nonzero(np.diff(row))[0].astype(np.int32)
+    og = O.Graph(row, adj, w, lab)
+    g = E.Graph(row, adj, w, lab)
+    try:
+        for schema, fat in (([0, 1, 2, 3, 4], True), ([3, 1, 4], True), ([2, 9, 1], True),
+                            ([0, 1, 0, 2], False), ([0, 1, 2, 3, 4], True)):
+            d = O.make_desc("metapath", "dynamic", "its", length=14, schema=schema, seed=23)
+            ref = O.walk(og, d, src, path_cap=14, want_counts=True)
+            r = E.compute(g, src, E.MetaPath(14, schema), seed=23, count_visits=True)
+            np.testing.assert_array_equal(r.paths.cpu().numpy(), ref["paths"], err_msg=str(schema))
+            np.testing.assert_array_equal(r.lengths.cpu().numpy(), ref["lengths"])
+            np.testing.assert_array_equal(r.counts.cpu().numpy(), ref["counts"][0])
+            assert r.steps == ref["steps"]
+            state = g.layout()[1]
+            if mode == "1" and fat:
+                assert state == 1
+            elif mode == "0":
+                assert state == -1
+    finally:
+        g.close()

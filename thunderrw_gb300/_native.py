@@ -59,7 +59,7 @@ def load(path: str = LIB_PATH):
     L.trw_graph_info.argtypes = [P, P, P, P]
     L.trw_graph_synchronize.argtypes = [P]
     L.trw_graph_indexes.argtypes = [P, P, P]
-    L.trw_graph_layout.argtypes = [P, P]
+    L.trw_graph_layout.argtypes = [P, P, P]
     L.trw_graph_build_indexes.argtypes = [P, I32, I32, P]
     L.trw_tables_build.argtypes = [P, I32, I32, P]
     L.trw_tables_download.argtypes = [P, I32, P, ctypes.c_size_t]

@@ -135,14 +135,19 @@ def metapath(paths: np.ndarray, row: np.ndarray, length: int) -> float:
     return (float((SECTOR + lab + SECTOR + 4).sum()) + tail) / frm.size
 
 
-def metapath_index(paths: np.ndarray, row: np.ndarray, length: int) -> float:
+def metapath_index(paths: np.ndarray, row: np.ndarray, length: int, fat: bool = False) -> float:
     """Bytes per move of MetaPath walks answered from the label index: the
     wanted label's two CSR positions, one sorted neighbour and the path
     entry (no row pair; a walk that stops early is charged the positions
-    read at its last vertex)."""
+    read at its last vertex).  ``fat``: the index entries carry the next
+    step's positions, so a move reads its entry's sector and the path entry;
+    only a walker's source positions are read (at its admission)."""
     frm, to, k, p = _moves(paths)
     if frm.size == 0:
         return 0.0
+    if fat:
+        walkers = int((np.asarray(p)[:, 0] >= 0).sum())
+        return (frm.size * (SECTOR + 4) + SECTOR * walkers) / frm.size
     last = _stops(p, length)
     return (frm.size * (SECTOR * 2 + 4) + SECTOR * last.size) / frm.size
 

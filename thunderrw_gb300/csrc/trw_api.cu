@@ -135,6 +135,12 @@ struct trw_graph {
     // built (the walks then read the row pairs)
     int4 *fat = nullptr;
     int fat_state = 0;
+    // the label index with the next step's positions (DevGraph::lab_fat),
+    // built by trw_walk for the schema in lab_fat_schema; lab_fat_state 0 =
+    // never decided, 1 = built (for that schema), -1 = not built
+    int4 *lab_fat = nullptr;
+    int lab_fat_state = 0;
+    std::vector<int32_t> lab_fat_schema;
     // engine state block: [kEngineSlots x (queue, steps)] + error word
     unsigned long long *state = nullptr;
     int *error = nullptr;
@@ -175,7 +181,7 @@ void destroy_graph(trw_graph *g) {
     if (!g) return;
     cudaFree(g->rows); cudaFree(g->adj); cudaFree(g->weight); cudaFree(g->label);
     cudaFree(g->alias); cudaFree(g->prefix); cudaFree(g->rmax); cudaFree(g->state); cudaFree(g->edges);
-    cudaFree(g->long_rows); cudaFree(g->lab_nbr); cudaFree(g->lab_off); cudaFree(g->fat);
+    cudaFree(g->long_rows); cudaFree(g->lab_nbr); cudaFree(g->lab_off); cudaFree(g->fat); cudaFree(g->lab_fat);
     for (auto &s : g->slots) if (s.done) cudaEventDestroy(s.done);
     if (g->scratch_done) cudaEventDestroy(g->scratch_done);
     for (cudaEvent_t e : {g->ev_walk0, g->ev_walk1, g->ev_post1, g->ppr_done, g->tables_done})
@@ -203,6 +209,7 @@ DevGraph dev_view(const trw_graph *g) {
     d.lab_off = g->lab_state == 1 ? g->lab_off : nullptr;
     d.lab_k = g->lab_state == 1 ? g->lab_k : 0;
     d.fat = g->fat_state == 1 ? g->fat : nullptr;
+    d.lab_fat = nullptr;  // per walk: lab_fat_for()
     return d;
 }
 
@@ -391,6 +398,71 @@ struct Plan {
     int weight_kind = kUnitWeight;
     int table_kind = -1;  // static table weights the run needs
 };
+
+// The walk's schema, if it names each label at most once (the label an
+// edge carries then fixes the label the next step wants): next[l] for every
+// label l < K, -1 where l is not in the schema or the label after it has no
+// edges.
+bool schema_next(const trw_walk_desc *d, int32_t K, LabelNext &next, std::vector<int32_t> &schema) {
+    schema.assign(d->schema, d->schema + std::max(0, d->schema_len));
+    if (schema.empty()) return false;
+    for (int32_t l = 0; l < kMaxIndexedLabels; ++l) next.label[l] = -1;
+    for (size_t i = 0; i < schema.size(); ++i) {
+        const int32_t l = schema[i];
+        for (size_t j = 0; j < i; ++j)
+            if (schema[j] == l) return false;
+        const int32_t w = schema[(i + 1) % schema.size()];
+        if (l >= 0 && l < K) next.label[l] = (w >= 0 && w < K) ? w : -1;
+    }
+    return true;
+}
+
+// Builds (or rebuilds, for another schema) DevGraph::lab_fat when the label
+// offsets (4 (K + 1) bytes per vertex) outgrow half the L2, so that their
+// read is DRAM traffic: a step then reads one 16-byte entry instead of its
+// block's positions and then the neighbour.  TRW_FAT_ADJACENCY=1 / 0 forces
+// it on / off.  Waits for the device before overwriting an index that an
+// earlier walk on any stream may still read.
+int prepare_lab_fat(trw_graph *g, const trw_walk_desc *desc, cudaStream_t st) {
+    if (g->lab_state != 1 || g->e <= 0) return TRW_OK;
+    LabelNext next;
+    std::vector<int32_t> schema;
+    if (!schema_next(desc, g->lab_k, next, schema)) return TRW_OK;
+    if (g->lab_fat_state == 1 && schema == g->lab_fat_schema) return TRW_OK;
+    if (g->lab_fat_state == 0) {
+        const char *force = getenv("TRW_FAT_ADJACENCY");
+        int l2 = 0;
+        TRW_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, g->device));
+        const size_t off_bytes = sizeof(int32_t) * (size_t)g->n * (size_t)(g->lab_k + 1);
+        const bool want = force && *force ? *force == '1' : off_bytes > (size_t)l2 / 2;
+        const size_t bytes = sizeof(int4) * (size_t)g->e;
+        size_t free_b = 0, total_b = 0;
+        TRW_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        if (!want || bytes + (size_t(1) << 30) > free_b || cudaMalloc(&g->lab_fat, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            g->lab_fat = nullptr;
+            g->lab_fat_state = -1;
+            return TRW_OK;
+        }
+    } else if (g->lab_fat_state == 1) {
+        TRW_CUDA(cudaDeviceSynchronize());  // another schema's walks may still read it
+        g->lab_fat_state = 0;
+    } else {
+        return TRW_OK;  // decided against
+    }
+    TRW_CUDA(launch_build_lab_fat(dev_view(g), next, g->lab_fat, st));
+    TRW_CUDA(cudaStreamSynchronize(st));
+    g->lab_fat_schema = schema;
+    g->lab_fat_state = 1;
+    return TRW_OK;
+}
+
+// DevGraph::lab_fat for a walk with this schema, or null.
+const int4 *lab_fat_for(const trw_graph *g, const trw_walk_desc *desc) {
+    if (g->lab_fat_state != 1) return nullptr;
+    const std::vector<int32_t> schema(desc->schema, desc->schema + std::max(0, desc->schema_len));
+    return schema == g->lab_fat_schema ? g->lab_fat : nullptr;
+}
 
 int make_plan(const trw_graph *g, const trw_walk_desc *d, Plan &pl) {
     if (d->app < 0 || d->app > 4) return fail(TRW_ERR_INVALID, "unknown app %d", d->app);
@@ -583,6 +655,10 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     TRW_CUDA(cudaSetDevice(g->device));
     rc = prepare_plan(g, desc, pl, st);
     if (rc) return rc;
+    if (pl.sampler == kLabelIndex) {
+        rc = prepare_lab_fat(g, desc, st);
+        if (rc) return rc;
+    }
 
     // Stage host buffers.
     const bool h_src = sources && !is_device_ptr(sources);
@@ -625,6 +701,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     WalkParams p;
     std::memset(&p, 0, sizeof p);
     p.g = dev_view(g);
+    if (pl.sampler == kLabelIndex) p.g.lab_fat = lab_fat_for(g, desc);
     fill_app_params(p, desc);
     p.static_unit = pl.table_kind == TRW_WEIGHTS_UNIT;
     p.sources = d_src;
@@ -882,9 +959,10 @@ int trw_graph_indexes(const trw_graph *g, int32_t *edge_set_state, int32_t *labe
     return TRW_OK;
 }
 
-int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state) {
-    if (!g || !fat_adjacency_state) return fail(TRW_ERR_INVALID, "null argument");
-    *fat_adjacency_state = g->fat_state;
+int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state, int32_t *fat_label_index_state) {
+    if (!g) return fail(TRW_ERR_INVALID, "null graph");
+    if (fat_adjacency_state) *fat_adjacency_state = g->fat_state;
+    if (fat_label_index_state) *fat_label_index_state = g->lab_fat_state;
     return TRW_OK;
 }
 
@@ -1290,6 +1368,7 @@ int trw::batch_walk(trw_graph *g, std::vector<BatchItem> &items, cudaStream_t st
             const Plan &pl = plans[(size_t)shared[a + (size_t)j].second];
             WalkParams &p = hp[j];
             p.g = dev_view(g);
+            if (pl.sampler == kLabelIndex) p.g.lab_fat = lab_fat_for(g, &it.desc);
             fill_app_params(p, &it.desc);
             p.static_unit = pl.table_kind == TRW_WEIGHTS_UNIT;
             p.sources = it.sources;

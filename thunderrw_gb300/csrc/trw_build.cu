@@ -420,6 +420,32 @@ __global__ void build_edge_set_kernel(DevGraph g, unsigned long long *set, int32
     }
 }
 
+// DevGraph::lab_fat: one warp per row, label block by label block; the
+// next label of block l is next.label[l] (-1: not in the schema, or no edge
+// carries it).
+__global__ void build_lab_fat_kernel(const DevGraph g, const LabelNext next, int4 *fat) {
+    const int lane = threadIdx.x & 31;
+    const int K = g.lab_k;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < g.n; v += warps) {
+        const int32_t *o = g.lab_off + v * (int64_t)(K + 1);
+        for (int32_t l = 0; l < K; ++l) {
+            const int32_t w = next.label[l];
+            const int32_t b = __ldg(o + l), end = __ldg(o + l + 1);
+            for (int32_t i = b + lane; i < end; i += 32) {
+                const int32_t u = __ldg(g.lab_nbr + i);
+                int32_t x = 0, y = 0;
+                if (w >= 0) {
+                    const int32_t *ou = g.lab_off + (int64_t)u * (K + 1) + w;
+                    x = __ldg(ou);
+                    y = __ldg(ou + 1);
+                }
+                fat[i] = make_int4(u, x, y, 0);
+            }
+        }
+    }
+}
+
 // The uniform moves' adjacency with the neighbours' row pairs (DevGraph::fat).
 __global__ void build_fat_kernel(DevGraph g, int4 *fat) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -504,6 +530,13 @@ cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, in
     gs.edges = set;
     gs.edge_bits = bits;
     edge_symmetry_kernel<<<grid, 256, 0, st>>>(gs, symmetric);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_lab_fat(const DevGraph &g, const LabelNext &next, int4 *fat, cudaStream_t st) {
+    if (g.n <= 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>(((int64_t)g.n * 32 + 255) / 256, 152 * 64);
+    build_lab_fat_kernel<<<(unsigned)blocks, 256, 0, st>>>(g, next, fat);
     return cudaGetLastError();
 }
 

@@ -108,6 +108,14 @@ struct DevGraph {
     const int32_t *lab_nbr;
     const int32_t *lab_off;
     int32_t lab_k;
+    // The label index with the next step's positions folded in, for a walk
+    // whose schema names each label at most once (so the label an entry's
+    // edge carries fixes the label its vertex's next step wants): entry j =
+    // {lab_nbr[j], lab_off[v * (lab_k + 1) + w], lab_off[... + w + 1], 0}
+    // with v = lab_nbr[j] and w the label after j's in the schema ({v, 0, 0}
+    // if w has no edges); one 16-byte load gives a step its vertex and the
+    // next step's block (null unless built for this walk's schema).
+    const int4 *lab_fat;
     // The adjacency with the row pairs folded in, for uniform and max-weight
     // rejection moves on graphs whose row pairs do not stay in L2: entry i
     // holds {adj[i], rows[adj[i]].x, rows[adj[i]].y, 0}, so one 16-byte load

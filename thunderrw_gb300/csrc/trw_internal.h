@@ -80,6 +80,12 @@ cudaError_t launch_build_label_index(const DevGraph &g, int32_t K, int32_t *off,
 // *symmetric must hold 1 and is cleared if some edge's reverse is missing.
 cudaError_t launch_build_edge_set(const DevGraph &g, unsigned long long *set, int32_t bits, int *symmetric,
                                   cudaStream_t st);
+// DevGraph::lab_fat for every label-index entry (g.lab_off / g.lab_nbr
+// read): label[l] = the label a step wants after one along a label-l edge
+struct LabelNext {
+    int32_t label[kMaxIndexedLabels];
+};
+cudaError_t launch_build_lab_fat(const DevGraph &g, const LabelNext &next, int4 *fat, cudaStream_t st);
 // DevGraph::fat for every edge (g.rows and g.adj are read)
 cudaError_t launch_build_fat(const DevGraph &g, int4 *fat, cudaStream_t st);
 cudaError_t launch_build_prefix(const DevGraph &g, int unit, double *out, const int32_t *long_rows,

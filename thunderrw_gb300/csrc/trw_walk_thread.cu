@@ -38,9 +38,11 @@ __device__ __forceinline__ void finish(const WalkParams &p, Slot &s) {
     s.widx = -1;
 }
 
-// kFat: the walk moves through DevGraph::fat when it is built, so the slot
-// carries the current vertex's row pair (read here for the source).
-template <bool kFat>
+// Sampler S moving through DevGraph::fat or DevGraph::lab_fat when they are
+// there: the slot then carries the current vertex's row pair, or for the
+// label index its first step's block of positions (read here for the
+// source).
+template <int S>
 __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx) {
     int64_t q = 0;
     int32_t src;
@@ -59,7 +61,15 @@ __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx)
         return;
     }
     s.cur = src;
-    if (kFat && p.g.fat) s.crow = __ldg(p.g.rows + src);
+    if ((S == kUniform || S == kMaxRejection) && p.g.fat) s.crow = __ldg(p.g.rows + src);
+    if (S == kLabelIndex && p.g.lab_fat) {
+        const int32_t want = p.schema[0];
+        s.crow = make_int2(0, 0);  // a label no edge has: no match
+        if (want >= 0 && want < p.g.lab_k) {
+            const int32_t *off = p.g.lab_off + (int64_t)src * (p.g.lab_k + 1) + want;
+            s.crow = make_int2(__ldg(off), __ldg(off + 1));
+        }
+    }
 }
 
 __device__ __forceinline__ AliasSlot load_alias(const AliasSlot *a) {
@@ -170,9 +180,11 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
                                           PendingInsert (&pend)[R][kInsertDepth]) {
     const DevGraph &g = p.g;
     // uniform and max-weight rejection moves through the adjacency with row
-    // pairs: the slot already holds the current row, and the entry a move
-    // takes brings the next one with its vertex
-    const bool fat = (S == kUniform || S == kMaxRejection) && g.fat != nullptr;
+    // pairs, label-index moves through the index with the next positions: the
+    // slot already holds the current row (block), and the entry a move takes
+    // brings the next one with its vertex
+    const bool fat = ((S == kUniform || S == kMaxRejection) && g.fat != nullptr) ||
+                     (S == kLabelIndex && g.lab_fat != nullptr);
     int32_t nxt[R];
     int2 nrow[R];
     bool moved[R];
@@ -275,6 +287,11 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         for (int r = 0; r < R; ++r) {
             cnt[r] = 0;
             if (s[r].widx < 0) continue;
+            if (fat) {  // the block came with the entry of the last move (or at admission)
+                lo[r] = s[r].crow.x;
+                cnt[r] = s[r].crow.y - s[r].crow.x;
+                continue;
+            }
             const int32_t want = p.schema[(s[r].len - 1) % p.schema_len];
             if (want < 0 || want >= g.lab_k) continue;  // a label no edge has: no match
             const int32_t *off = g.lab_off + (int64_t)s[r].cur * (g.lab_k + 1) + want;
@@ -285,7 +302,13 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         for (int r = 0; r < R; ++r) {
             if (cnt[r] <= 0) continue;
             const int32_t m = (int32_t)((double)cnt[r] * real2(rnd[r].x));  // floor of P[last] * dr_
-            nxt[r] = __ldg(g.lab_nbr + lo[r] + m);
+            if (fat) {
+                const int4 f = __ldg(g.lab_fat + lo[r] + m);
+                nxt[r] = f.x;
+                nrow[r] = make_int2(f.y, f.z);
+            } else {
+                nxt[r] = __ldg(g.lab_nbr + lo[r] + m);
+            }
             moved[r] = true;
         }
     } else if (S == kRejection) {
@@ -414,7 +437,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
                 const unsigned avail = (unsigned)min(res_end - res_next, 32ull);
                 const unsigned rank = __popc(need & lanemask_lt());
                 const bool mine = ((need >> lane) & 1u) && rank < avail;
-                if (mine) admit<S == kUniform || S == kMaxRejection>(p, s[r], (int64_t)(res_next + rank));
+                if (mine) admit<S>(p, s[r], (int64_t)(res_next + rank));
                 res_next += min((unsigned)__popc(need), avail);
                 need &= ~__ballot_sync(kFull, mine);
             }
@@ -442,7 +465,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
         Slot s[1];
         PendingInsert pend[1][kInsertDepth];
             for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
-        admit<S == kUniform || S == kMaxRejection>(p, s[0], idx);
+        admit<S>(p, s[0], idx);
         while (s[0].widx >= 0) step_ring<S, U, WK, 1, kSparse>(p, s, steps, pend);
         if (kSparse)
             for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[0][k], true);
@@ -495,7 +518,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_multi(const MultiBatch mb, 
             if (mine) {
                 req = r_req;
                 wsteps = 0;
-                admit<S == kUniform || S == kMaxRejection>(mb.reqs[req], s[0], r_next + rank);
+                admit<S>(mb.reqs[req], s[0], r_next + rank);
                 dead = s[0].widx < 0;  // an invalid source finishes at once
             }
             if (dead) {

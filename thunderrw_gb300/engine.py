@@ -199,13 +199,18 @@ class Graph:
         N.check(_lib().trw_graph_indexes(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def layout(self):
+        """(fat adjacency, fat label index) states: 1 if the uniform and
+        max-weight rejection walks read the 16-byte adjacency entries carrying
+        each neighbour's row pair / if MetaPath walks with the last
+        unique-label schema read label-index entries carrying the next step's
+        block, -1 if not, 0 if no walk has decided it yet."""
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        N.check(_lib().trw_graph_layout(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def fat_adjacency(self) -> int:
-        """1 if the uniform and max-weight rejection walks read the 16-byte
-        adjacency entries carrying each neighbour's row pair, -1 if they read
-        the plain adjacency, 0 if no such walk has decided it yet."""
-        a = ctypes.c_int32()
-        N.check(_lib().trw_graph_layout(self._h, ctypes.byref(a)))
-        return a.value
+        return self.layout()[0]
 
     def build_indexes(self, edge_set: bool = True, label_index: bool = True, stream=None):
         """Builds the Node2Vec edge set and / or the MetaPath label index now
