@@ -473,7 +473,9 @@ def measure(name, args, over, dev, rank, world, steps, warmup, headline):
         shape = {"slot": tr.sampler, "walkers_per_lane": tr.best[0], "ctas_per_sm": tr.best[1],
                  "tuned_on_walkers": tr.walkers, "candidates": len(tr.timings)}
         torch.cuda.synchronize()
-    res["engine"] = {"engine": "persistent", "launch_shape": shape,
+    plain_shape = isinstance(shape, dict) and shape["walkers_per_lane"] == -1
+    res["engine"] = {"engine": "plain form (the tuned launch shape)" if plain_shape else "persistent",
+                     "launch_shape": shape,
                      "output": ("sparse CSR per query (offsets, vertex, int32 count)" if sparse else
                                 "dense int32 [Q][N], zeroed every step" if name == "ppr" else
                                 "int32 paths [W][L] + lengths")}

@@ -248,7 +248,11 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
 /* Launch shape of the persistent engine for this graph and sampler: walkers
  * per thread (ring depth 1, 2, 4 or 8) and CTAs per SM.  0 = automatic (ring
  * 1 for sparse PPR tables or fewer than 4 x SMs x 2048 walkers, else 4; as
- * many CTAs as fit).  thunderrw_gb300/autotune.py measures and sets them. */
+ * many CTAs as fit).  walkers_per_thread = -1 makes persistent-engine calls
+ * with this sampler run the plain form instead (one thread per walker, no
+ * refill: the form some fixed-length walks run fastest in; the warp-family
+ * kernels keep their own).  thunderrw_gb300/autotune.py measures and sets
+ * them.  Walks are the same under every shape. */
 int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm);
 int trw_get_engine_shape(const trw_graph *g, int32_t sampler, int32_t *walkers_per_thread,
                          int32_t *ctas_per_sm);

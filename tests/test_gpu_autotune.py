@@ -19,7 +19,7 @@ def test_tune_sets_fastest_shape_and_keeps_results():
         app = E.DeepWalk(12)
         before = E.compute(graph, src, app, seed=5)
         res = autotune.tune(graph, app, src, rings=(1, 4), ctas=(0, 2), repeats=1)
-        assert set(res.timings) == {(0, 0), (1, 0), (1, 2), (4, 0), (4, 2)}
+        assert set(res.timings) == {(0, 0), (1, 0), (1, 2), (4, 0), (4, 2), (-1, 0)}
         fastest = min(res.timings, key=res.timings.get)
         # the automatic shape stays unless beaten by more than 3 %
         assert res.best in (fastest, (0, 0))
@@ -29,14 +29,19 @@ def test_tune_sets_fastest_shape_and_keeps_results():
         assert torch.equal(before.paths, after.paths) and before.steps == after.steps
         # sparse PPR tunes the uniform slot
         r2 = autotune.tune(graph, E.PPR(0.2), src[:8], walkers_per_query=2000, rings=(1, 2), ctas=(0,), repeats=1)
-        assert r2.sampler == "uniform" and set(r2.timings) == {(0, 0), (1, 0), (2, 0)}
+        assert r2.sampler == "uniform" and set(r2.timings) == {(0, 0), (1, 0), (2, 0), (-1, 0)}
         # Node2Vec's dynamic ITS (walker-dependent weights, one warp per walker step): CTAs only
         r3 = autotune.tune(graph, E.Node2Vec(6, 2.0, 0.5, sampler="its"), src, ctas=(0, 1), repeats=1)
         assert r3.sampler == "its" and set(r3.timings) == {(0, 0), (0, 1)}
         # DeepWalk's dynamic ITS runs on the static tables: rings are tuned too
         r4 = autotune.tune(graph, E.DeepWalk(6, mode="dynamic", sampler="its"), src, rings=(1, 2), ctas=(0,),
                            repeats=1)
-        assert set(r4.timings) == {(0, 0), (1, 0), (2, 0)}
+        assert set(r4.timings) == {(0, 0), (1, 0), (2, 0), (-1, 0)}
         assert np.isfinite(list(r3.timings.values())).all()
+        # the plain form as a tuned shape: same walks
+        graph.set_engine_shape("alias", -1, 0)
+        plain = E.compute(graph, src, app, seed=5)
+        assert torch.equal(before.paths, plain.paths) and before.steps == plain.steps
+        assert graph.engine_shape("alias") == (-1, 0)
     finally:
         graph.close()

@@ -3,7 +3,9 @@
 The reference fixes its ring (RING_SIZE = 64 slots per thread, 32 search
 frames, creeper.h / types.h) at compile time.  Here the equivalent knobs are
 runtime launch shapes of the persistent engine: walkers in flight per lane
-(the ring depth R, 1/2/4/8) and CTAs per SM.  Which shape is fastest depends
+(the ring depth R, 1/2/4/8) and CTAs per SM, or the plain form (one thread
+per walker, no refill; shape (-1, 0)), which some fixed-length walks run
+fastest in.  Which shape is fastest depends
 on the graph's degree profile and the app: sparse-table PPR and max-weight
 rejection want R = 1, static alias R = 4 on large batches, and a batch of
 about one walker per lane (DeepWalk on Chung-Lu 2^18) runs fastest with 4
@@ -50,7 +52,7 @@ def tune(graph: E.Graph, app: E.App, sources, walkers_per_query: int = 0, mode: 
          sampler: Optional[str] = None, rings: Sequence[int] = (1, 2, 4, 8),
          ctas: Sequence[int] = (0, 2, 4, 8), sample_walkers: Optional[int] = None, repeats: int = 3,
          record_paths: bool = True, seed: int = 12345, apply: bool = True,
-         tolerance: float = 0.03) -> TuneResult:
+         tolerance: float = 0.03, plain: bool = True) -> TuneResult:
     """Times every (ring, CTAs/SM) candidate on a sample of the workload and
     keeps the fastest.  `walkers_per_query` > 0 tunes sparse batched PPR
     (`sources` are then the queries).  The sample keeps at least 16 walkers
@@ -76,6 +78,8 @@ def tune(graph: E.Graph, app: E.App, sources, walkers_per_query: int = 0, mode: 
         for c in ctas:
             if (r, c) not in cands:
                 cands.append((r, c))
+    if plain and not warp_family:
+        cands.append((-1, 0))
     old = graph.engine_shape(slot)
     stream = torch.cuda.current_stream(dev)
 

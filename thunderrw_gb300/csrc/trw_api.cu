@@ -721,6 +721,10 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     LaunchShape shape = g->shape[pl.sampler == kLabelIndex ? (int)kITS : pl.sampler];
     shape.engine = engine;
     shape.num_sms = g->num_sms;
+    if (shape.ring < 0) {  // the shape set for this sampler is the plain form (one thread per walker)
+        if (!pl.warp_family) shape.engine = kEnginePlain;
+        shape.ring = 0;
+    }
     if (shape.ring == 0) {
         // Automatic ring depth (launch-shape sweeps on GB300): one walker per
         // lane when visits go to sparse tables (their insert records cost
@@ -1268,10 +1272,10 @@ int trw_profile_read(trw_graph *g, float *walk_ms, float *post_ms) {
 int trw_set_engine_shape(trw_graph *g, int32_t sampler, int32_t walkers_per_thread, int32_t ctas_per_sm) {
     if (!g || sampler < 0 || sampler > 4) return fail(TRW_ERR_INVALID, "bad arguments");
     if (walkers_per_thread != 0 && walkers_per_thread != 1 && walkers_per_thread != 2 && walkers_per_thread != 4 &&
-        walkers_per_thread != 8)
-        return fail(TRW_ERR_INVALID, "walkers per thread must be 1, 2, 4 or 8");
+        walkers_per_thread != 8 && walkers_per_thread != -1)
+        return fail(TRW_ERR_INVALID, "walkers per thread must be 1, 2, 4 or 8 (0 automatic, -1 the plain form)");
     std::lock_guard<std::mutex> lock(g->mu);
-    g->shape[sampler].ring = walkers_per_thread;  // 0 = automatic
+    g->shape[sampler].ring = walkers_per_thread;  // 0 = automatic, -1 = the plain form
     g->shape[sampler].ctas_per_sm = ctas_per_sm > 0 ? ctas_per_sm : 0;
     return TRW_OK;
 }
