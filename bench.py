@@ -55,16 +55,16 @@ BYTES_PER_STEP = {
 # workload's walk kernel, from one ncu capture of that kernel: PPR on the
 # full N = 2^22 graph with 256 queries (1.386 GB over 12.80 M steps; the full
 # batch's tables do not change the per-step traffic of the walk: only the
-# in-flight queries' tables are written), DeepWalk and Node2Vec on their full
-# graphs (Node2Vec with the adjacency entries that carry row pairs), MetaPath
-# on an R-MAT 2^22 instance of its graph.  Scaled by the steps of one full
-# launch.
+# in-flight queries' tables are written), DeepWalk, Node2Vec and MetaPath on
+# their full graphs (Node2Vec and MetaPath in the plain form the autotuner
+# picks, with the 16-byte entries that carry the next step's row or block).
+# Scaled by the steps of one full launch.
 TRAFFIC_BYTES_PER_STEP = {
     "ppr": 108.25,
     "ppr_dense": 89.13,
     "deepwalk": 16.47,
-    "node2vec": 207.78,
-    "metapath": 155.1,
+    "node2vec": 209.88,
+    "metapath": 150.24,
 }
 
 WORKLOADS = {
