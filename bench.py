@@ -62,7 +62,7 @@ BYTES_PER_STEP = {
 TRAFFIC_BYTES_PER_STEP = {
     "ppr": 108.25,
     "ppr_dense": 89.13,
-    "deepwalk": 16.47,
+    "deepwalk": 26.02,
     "node2vec": 209.88,
     "metapath": 150.24,
 }
