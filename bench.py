@@ -792,7 +792,8 @@ def run_serving(args):
                                    "index resident; PPR/DeepWalk/Node2Vec/MetaPath uniform, walkers log-uniform "
                                    "1e3-1e6, L 5-80, Poisson arrivals" % scale,
                        "n": graph.n, "e": graph.e, "table_build_s": build_s, "max_inflight": args.inflight,
-                       "indexes": {"edge_set": indexes[0], "label_index": indexes[1]}},
+                       "indexes": {"edge_set": indexes[0], "label_index": indexes[1],
+                                   "fat_adjacency": graph.layout()[0]}},
             "serving": results}
     print(json.dumps(line), flush=True)
     graph.close()

@@ -157,7 +157,9 @@ int trw_graph_layout(const trw_graph *g, int32_t *fat_adjacency_state, int32_t *
  * build (the reference builds everything it needs before compute() starts
  * its timer, creeper.h:700-766).  Nonzero flags select the structures; one
  * already built, not applicable or without room is left as it is (read the
- * states with trw_graph_indexes).  Synchronises the stream. */
+ * states with trw_graph_indexes).  edge_set also decides and builds the
+ * adjacency entries with row pairs (trw_graph_layout).  Synchronises the
+ * stream. */
 int trw_graph_build_indexes(trw_graph *g, int32_t edge_set, int32_t label_index, trw_stream_t stream);
 
 /* ---- static tables ---------------------------------------------------- */

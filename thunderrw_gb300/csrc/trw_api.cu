@@ -976,7 +976,9 @@ int trw_graph_build_indexes(trw_graph *g, int32_t edge_set, int32_t label_index,
     TRW_CUDA(cudaSetDevice(g->device));
     const cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (edge_set) {
-        const int rc = build_edge_set(g, st);
+        int rc = build_edge_set(g, st);
+        if (rc) return rc;
+        rc = build_fat_adjacency(g, st);  // decided by the same rule as in a walk
         if (rc) return rc;
     }
     if (label_index) {
