@@ -53,14 +53,14 @@ BYTES_PER_STEP = {
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per step of each
 # workload's walk kernel, from one ncu capture of that kernel: PPR on the
-# full N = 2^22 graph with 256 queries (1.386 GB over 12.80 M steps; the full
+# full N = 2^22 graph with 256 queries (1.259 GB over 12.80 M steps; the full
 # batch's tables do not change the per-step traffic of the walk: only the
 # in-flight queries' tables are written), DeepWalk, Node2Vec and MetaPath on
 # their full graphs (Node2Vec and MetaPath in the plain form the autotuner
 # picks, with the 16-byte entries that carry the next step's row or block).
 # Scaled by the steps of one full launch.
 TRAFFIC_BYTES_PER_STEP = {
-    "ppr": 108.25,
+    "ppr": 98.34,
     "ppr_dense": 89.13,
     "deepwalk": 26.02,
     "node2vec": 209.88,

@@ -135,6 +135,7 @@ struct trw_graph {
     // built (the walks then read the row pairs)
     int4 *fat = nullptr;
     int fat_state = 0;
+    int32_t adj_streams = 0;  // DevGraph::adj_streams (set at creation)
     // the label index with the next step's positions (DevGraph::lab_fat),
     // built by trw_walk for the schema in lab_fat_schema; lab_fat_state 0 =
     // never decided, 1 = built (for that schema), -1 = not built
@@ -210,6 +211,7 @@ DevGraph dev_view(const trw_graph *g) {
     d.lab_k = g->lab_state == 1 ? g->lab_k : 0;
     d.fat = g->fat_state == 1 ? g->fat : nullptr;
     d.lab_fat = nullptr;  // per walk: lab_fat_for()
+    d.adj_streams = g->adj_streams;
     return d;
 }
 
@@ -893,6 +895,11 @@ int trw_graph_create(const int64_t *row_ptr, const int32_t *adj, const double *w
     cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device);
     g->n = n;
     g->e = e;
+    {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, g->device);
+        g->adj_streams = l2 > 0 && sizeof(int32_t) * (size_t)e >= 2 * (size_t)l2;
+    }
     const size_t es = (size_t)(e ? e : 1);
     int64_t *d_row = nullptr;
     int *d_flags = nullptr;

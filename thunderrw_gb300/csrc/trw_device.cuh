@@ -116,6 +116,8 @@ struct DevGraph {
     // if w has no edges); one 16-byte load gives a step its vertex and the
     // next step's block (null unless built for this walk's schema).
     const int4 *lab_fat;
+    // the adjacency is at least twice the L2: uniform moves read it evict-first
+    int32_t adj_streams;
     // The adjacency with the row pairs folded in, for uniform and max-weight
     // rejection moves on graphs whose row pairs do not stay in L2: entry i
     // holds {adj[i], rows[adj[i]].x, rows[adj[i]].y, 0}, so one 16-byte load
@@ -138,6 +140,53 @@ __device__ __forceinline__ uint32_t edge_slot(unsigned long long k, int32_t bits
 
 // Whether the directed edge (u, v) exists (u's list holds v).  The set is at
 // most two-thirds full, so a free slot ends every probe sequence.
+// L2 eviction priority (createpolicy + ld .L2::cache_hint, PTX ISA 7.4 for
+// sm_80 and later).  On a graph whose adjacency is several times the L2, a
+// uniform step's random adjacency read brings in a fresh line (about
+// 2.4 TB/s of them in the sparse PPR walk) that is rarely read again before
+// it leaves L2; marked evict-first it stops pushing out the lines that are
+// read again: the in-flight queries' visit tables (whose key loads are
+// marked evict-last) and the hot rows.  Measured on GB300: the sparse PPR
+// walk on R-MAT 2^22 (0.5 GB of adjacency) 5.55 -> 5.14 ms.  Where the data
+// is re-read from L2 the same hint costs: DeepWalk on Chung-Lu 2^18 (graph
+// and alias table in L2) 0.27 -> 0.41 ms with its alias reads marked,
+// Node2Vec 22.5 -> 23.3 ms with its candidate and edge-set reads marked; so
+// only the uniform move's adjacency read takes it, and only on such graphs.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+// read-only data read once (the non-coherent path, evict-first in L2)
+__device__ __forceinline__ int32_t ld_once(const int32_t *a) {
+    int32_t v;
+    asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_evict_first()));
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_once(const unsigned long long *a) {
+    unsigned long long v;
+    asm volatile("ld.global.nc.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(l2_evict_first()));
+    return v;
+}
+__device__ __forceinline__ int4 ld_once(const int4 *a) {
+    int4 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(a), "l"(l2_evict_first()));
+    return v;
+}
+// data written by atomics during the kernel, read through L2 and kept there
+__device__ __forceinline__ int32_t ldcg_keep(const int32_t *a) {
+    int32_t v;
+    asm volatile("ld.global.cg.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_evict_last()));
+    return v;
+}
+
 __device__ __forceinline__ bool edge_exists(const DevGraph &g, int32_t u, int32_t v) {
     const unsigned long long k = edge_key(u, v);
     const uint32_t mask = (1u << g.edge_bits) - 1u;

@@ -159,7 +159,7 @@ __device__ __forceinline__ void resolve(const WalkParams &p, PendingInsert &pi, 
         }
         pi.meta = (pi.meta & kIncMask) + ((probes + 1) << 7);  // cas bit cleared
         pi.h = (pi.h + 1) & mask;
-        pi.old = __ldcg(t + pi.h);
+        pi.old = ldcg_keep(t + pi.h);
         if (!blocking) return;
     }
 }
@@ -170,7 +170,7 @@ __device__ __forceinline__ void start_insert(const WalkParams &p, PendingInsert 
     pi.h = ((uint32_t)v * 0x9E3779B1u) >> (32 - p.table_bits);
     pi.key = v + 1;
     pi.meta = (uint32_t)inc;
-    pi.old = __ldcg(table_of(p, pi.q) + pi.h);
+    pi.old = ldcg_keep(table_of(p, pi.q) + pi.h);
 }
 
 // One step for each of the R slots, stage by stage.  kSparse: visits go to
@@ -215,12 +215,13 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
             const int32_t deg = s[r].crow.y - s[r].crow.x;
             if (deg <= 0) continue;
             const int32_t at = s[r].crow.x + (int32_t)(rnd[r].x % (uint32_t)deg);
+            // (evict-first in L2 where the adjacency dwarfs it: DevGraph::adj_streams)
             if (fat) {
-                const int4 f = __ldg(g.fat + at);
+                const int4 f = g.adj_streams ? ld_once(g.fat + at) : __ldg(g.fat + at);
                 nxt[r] = f.x;
                 nrow[r] = make_int2(f.y, f.z);
             } else {
-                nxt[r] = __ldg(g.adj + at);
+                nxt[r] = g.adj_streams ? ld_once(g.adj + at) : __ldg(g.adj + at);
             }
             moved[r] = true;
         }
