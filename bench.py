@@ -62,7 +62,7 @@ BYTES_PER_STEP = {
 TRAFFIC_BYTES_PER_STEP = {
     "ppr": 98.34,
     "ppr_dense": 89.13,
-    "deepwalk": 26.02,
+    "deepwalk": 20.75,
     "node2vec": 209.88,
     "metapath": 150.24,
 }

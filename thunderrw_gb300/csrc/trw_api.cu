@@ -712,6 +712,7 @@ int run_walk(trw_graph *g, const trw_walk_desc *desc, const int32_t *sources, in
     p.id_base = id_base;
     p.paths = d_paths;
     p.path_cap = paths ? path_cap : 0;
+    p.path_vec = d_paths && path_cap % 4 == 0 && reinterpret_cast<uintptr_t>(d_paths) % 16 == 0;
     p.lengths = d_len;
     p.counts = d_cnt;
     p.queue_head = slot.queue_head;
@@ -1390,6 +1391,7 @@ int trw::batch_walk(trw_graph *g, std::vector<BatchItem> &items, cudaStream_t st
             p.id_base = it.id_base;
             p.paths = it.paths;
             p.path_cap = it.paths ? it.path_cap : 0;
+            p.path_vec = it.paths && it.path_cap % 4 == 0 && reinterpret_cast<uintptr_t>(it.paths) % 16 == 0;
             p.lengths = it.lengths;
             p.steps = reinterpret_cast<unsigned long long *>(it.steps);
             p.error = g->error;

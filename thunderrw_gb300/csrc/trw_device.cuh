@@ -234,6 +234,7 @@ struct WalkParams {
     // outputs
     int32_t *paths;
     int32_t path_cap;
+    int32_t path_vec;     // paths 16-byte aligned and path_cap % 4 == 0: the thread kernels store 4 entries at a time
     int32_t *lengths;
     int32_t *counts;
     // engine state

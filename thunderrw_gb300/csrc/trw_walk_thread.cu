@@ -29,11 +29,74 @@ struct Slot {
     int2 crow, prow;  // row pairs of cur and prev
 };
 
-__device__ __forceinline__ void finish(const WalkParams &p, Slot &s) {
+// Path entries of the CTA's ring slots being gathered into groups of four
+// (WalkParams::path_vec): component c of slot r of thread t at
+// [(c * R + r) * kThreadBlock + t], so a warp's accesses hit distinct banks.
+template <int R>
+__device__ __forceinline__ int32_t *path_stage() {
+    __shared__ int32_t stage[4 * R * kThreadBlock];
+    return stage;
+}
+
+// Path entry k of ring slot r's walker.  With p.path_vec the entries of each
+// group of four gather in shared memory and leave as one 16-byte store: a
+// walker's path row then fills whole sectors instead of 4-byte pieces that
+// leave L2 half written (each such sector costs DRAM a read-modify-write).
+template <bool kVec, int R>
+__device__ __forceinline__ void path_put(const WalkParams &p, const Slot &s, int r, int32_t k, int32_t v) {
+    if (!kVec || !p.path_vec) {
+        p.paths[s.widx * (int64_t)p.path_cap + k] = v;
+        return;
+    }
+    int32_t *st = path_stage<R>() + r * kThreadBlock + threadIdx.x;
+    const int c = k & 3;
+    if (c < 3) {
+        st[c * R * kThreadBlock] = v;
+        return;
+    }
+    const int4 g = make_int4(st[0], st[R * kThreadBlock], st[2 * R * kThreadBlock], v);
+    *reinterpret_cast<int4 *>(p.paths + s.widx * (int64_t)p.path_cap + (k - 3)) = g;
+}
+
+// The end of slot r's path: the pending group, then -1 up to path_cap
+// (out of line: walks that stop early are rare, and inlined at every finish
+// this code costs the step loop registers).
+template <bool kVec, int R>
+__device__ __noinline__ void finish_path(const WalkParams &p, int64_t widx, int32_t len, int r) {
+    int32_t *row = p.paths + widx * (int64_t)p.path_cap;
+    int32_t k = len;
+    if (!kVec || !p.path_vec) {
+        for (; k < p.path_cap; ++k) row[k] = -1;
+        return;
+    }
+    if (k >= p.path_cap) return;
+    if (k & 3) {  // the pending group: its gathered entries below k, then -1
+        const int c = k & 3;
+        const int32_t *st = path_stage<R>() + r * kThreadBlock + threadIdx.x;
+        const int4 g = make_int4(st[0], c > 1 ? st[R * kThreadBlock] : -1, c > 2 ? st[2 * R * kThreadBlock] : -1, -1);
+        *reinterpret_cast<int4 *>(row + (k & ~3)) = g;
+        k = (k + 3) & ~3;
+    }
+    for (; k < p.path_cap; k += 4) *reinterpret_cast<int4 *>(row + k) = make_int4(-1, -1, -1, -1);
+}
+
+// kVec: gather path entries (only the static alias walks: with the graph in
+// L2 their DRAM traffic is the paths; DeepWalk on Chung-Lu 2^18 0.270 ->
+// 0.245 ms, 26.0 -> 20.7 B/step.  Node2Vec and MetaPath lost 2 % to the
+// registers it takes.)
+template <int S>
+__host__ __device__ constexpr bool path_gather() { return S == kAlias; }
+
+template <bool kVec, int R>
+__device__ __forceinline__ void finish(const WalkParams &p, Slot &s, int r) {
     if (p.lengths) p.lengths[s.widx] = s.len;
     if (p.paths) {
-        int32_t *row = p.paths + s.widx * (int64_t)p.path_cap;
-        for (int32_t k = s.len; k < p.path_cap; ++k) row[k] = -1;
+        if (kVec) {
+            if (s.len < p.path_cap) finish_path<kVec, R>(p, s.widx, s.len, r);
+        } else {
+            int32_t *row = p.paths + s.widx * (int64_t)p.path_cap;
+            for (int32_t k = s.len; k < p.path_cap; ++k) row[k] = -1;
+        }
     }
     s.widx = -1;
 }
@@ -42,8 +105,8 @@ __device__ __forceinline__ void finish(const WalkParams &p, Slot &s) {
 // there: the slot then carries the current vertex's row pair, or for the
 // label index its first step's block of positions (read here for the
 // source).
-template <int S>
-__device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx) {
+template <int S, int R>
+__device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int r, int64_t idx) {
     int64_t q = 0;
     int32_t src;
     if (p.per_query > 0) { q = idx / p.per_query; src = __ldg(p.sources + q); }
@@ -53,11 +116,11 @@ __device__ __forceinline__ void admit(const WalkParams &p, Slot &s, int64_t idx)
     s.len = 1;
     s.prev = -1;
     s.prow = make_int2(0, 0);
-    if (p.paths && p.path_cap > 0) p.paths[idx * (int64_t)p.path_cap] = src;
+    if (p.paths && p.path_cap > 0) path_put<path_gather<S>(), R>(p, s, r, 0, src);
     if (src < 0 || src >= p.g.n) {  // rejected here so no kernel reads outside the graph
         atomicOr(p.error, kErrVertex);
         s.cur = 0;
-        finish(p, s);
+        finish<path_gather<S>(), R>(p, s, r);
         return;
     }
     s.cur = src;
@@ -382,12 +445,12 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         if (s[r].widx < 0) continue;
-        if (!moved[r]) { finish(p, s[r]); continue; }
+        if (!moved[r]) { finish<path_gather<S>(), R>(p, s[r], r); continue; }
         s[r].prev = s[r].cur;
         if (S != kLabelIndex) s[r].prow = s[r].crow;  // (the label index reads no row pair)
         s[r].cur = nxt[r];
         if (fat) s[r].crow = nrow[r];
-        if (p.paths && s[r].len < p.path_cap) p.paths[s[r].widx * (int64_t)p.path_cap + s[r].len] = nxt[r];
+        if (p.paths && s[r].len < p.path_cap) path_put<path_gather<S>(), R>(p, s[r], r, s[r].len, nxt[r]);
         s[r].len += 1;
         steps += 1;
         if (kSparse) {
@@ -396,7 +459,7 @@ __device__ __forceinline__ void step_ring(const WalkParams &p, Slot (&s)[R], uin
         } else {
             record_visit(p, s[r].q, nxt[r]);
         }
-        if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) finish(p, s[r]);
+        if (app_update<U>(p, (uint64_t)(p.id_base + s[r].widx), s[r].len)) finish<path_gather<S>(), R>(p, s[r], r);
     }
 }
 
@@ -438,7 +501,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_persistent(const WalkParams
                 const unsigned avail = (unsigned)min(res_end - res_next, 32ull);
                 const unsigned rank = __popc(need & lanemask_lt());
                 const bool mine = ((need >> lane) & 1u) && rank < avail;
-                if (mine) admit<S>(p, s[r], (int64_t)(res_next + rank));
+                if (mine) admit<S, R>(p, s[r], r, (int64_t)(res_next + rank));
                 res_next += min((unsigned)__popc(need), avail);
                 need &= ~__ballot_sync(kFull, mine);
             }
@@ -466,7 +529,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_plain(const WalkParams p) {
         Slot s[1];
         PendingInsert pend[1][kInsertDepth];
             for (int k = 0; k < kInsertDepth; ++k) pend[0][k].q = -1;
-        admit<S>(p, s[0], idx);
+        admit<S, 1>(p, s[0], 0, idx);
         while (s[0].widx >= 0) step_ring<S, U, WK, 1, kSparse>(p, s, steps, pend);
         if (kSparse)
             for (int k = 0; k < kInsertDepth; ++k) resolve(p, pend[0][k], true);
@@ -519,7 +582,7 @@ __global__ void __launch_bounds__(kThreadBlock) walk_multi(const MultiBatch mb, 
             if (mine) {
                 req = r_req;
                 wsteps = 0;
-                admit<S>(mb.reqs[req], s[0], r_next + rank);
+                admit<S, 1>(mb.reqs[req], s[0], 0, r_next + rank);
                 dead = s[0].widx < 0;  // an invalid source finishes at once
             }
             if (dead) {
