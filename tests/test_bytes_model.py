@@ -58,6 +58,12 @@ def test_metapath_index_model_equals_oracle(graph):
     walks = O.walk(graph, d, src, path_cap=10)
     nb, ns = O.count_bytes(graph, d, src, record_paths=True, label_index=True)
     assert B.metapath_index(walks["paths"], graph.row, 10) == pytest.approx(nb / ns, rel=1e-12)
+    # label-index entries carrying the next block: one sector and the path
+    # entry per move, plus each walker's source positions; no stop charge
+    moves = int(((walks["paths"][:, :-1] >= 0) & (walks["paths"][:, 1:] >= 0)).sum())
+    fat = B.metapath_index(walks["paths"], graph.row, 10, fat=True)
+    assert fat * moves == pytest.approx(moves * 36 + 32 * src.size)
+    assert fat < B.metapath_index(walks["paths"], graph.row, 10)
 
 
 def test_constant_models(graph):
