@@ -33,6 +33,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.gpu_util import need_gpu
+from tests.sparse_order import canonical, table_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -99,6 +100,8 @@ def test_ppr_batch_rmat_2e22_full_batch():
         assert vert.min() >= 0 and vert.max() < g.n
         og = O.Graph(host["row"], host["adj"])
         d = O.make_desc("ppr", "uniform", "uniform", length=1, tp=tp, seed=123)
+        bits = table_bits(pq, tp, g.n)
+        assert bits == 16
         for a, b in _ranges(Q, 24):
             ref = O.walk(og, d, host["sources"][a:b], per_query=pq, id_base=a * pq, want_counts=True,
                          want_lengths=False)
@@ -109,6 +112,8 @@ def test_ppr_batch_rmat_2e22_full_batch():
                 order = np.argsort(v)
                 assert np.array_equal(v[order], nz), q
                 assert np.array_equal(c[order], ref["counts"][q - a][nz]), q
+                # the emit's canonical order on the full-size (2^16-slot) table
+                assert np.array_equal(v, canonical(v, bits)), q
         assert g.device_error() == 0
     finally:
         g.close()
