@@ -56,13 +56,14 @@ BYTES_PER_STEP = {
 # full N = 2^22 graph with 256 queries (1.259 GB over 12.80 M steps; the full
 # batch's tables do not change the per-step traffic of the walk: only the
 # in-flight queries' tables are written), DeepWalk, Node2Vec and MetaPath on
-# their full graphs (Node2Vec and MetaPath in the plain form the autotuner
-# picks, with the 16-byte entries that carry the next step's row or block).
+# their full graphs (each in the form the autotuner picks: DeepWalk one
+# walker per lane and 4 CTAs per SM, Node2Vec and MetaPath the plain form
+# with the 16-byte entries that carry the next step's row or block).
 # Scaled by the steps of one full launch.
 TRAFFIC_BYTES_PER_STEP = {
     "ppr": 98.34,
     "ppr_dense": 89.13,
-    "deepwalk": 20.75,
+    "deepwalk": 14.01,
     "node2vec": 209.88,
     "metapath": 150.24,
 }
