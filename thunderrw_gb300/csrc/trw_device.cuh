@@ -168,11 +168,6 @@ __device__ __forceinline__ int32_t ld_once(const int32_t *a) {
     asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(l2_evict_first()));
     return v;
 }
-__device__ __forceinline__ unsigned long long ld_once(const unsigned long long *a) {
-    unsigned long long v;
-    asm volatile("ld.global.nc.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(l2_evict_first()));
-    return v;
-}
 __device__ __forceinline__ int4 ld_once(const int4 *a) {
     int4 v;
     asm volatile("ld.global.nc.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
