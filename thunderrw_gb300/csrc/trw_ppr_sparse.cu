@@ -144,10 +144,11 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 // in shared memory (the previous, current and next block, and the one after
 // being filled); four ballots per block give its 128-bit occupancy, from
 // which every slot finds the empty slots before and after its run with
-// clz/ffs over the 384-slot window, and it ranks its key by reading the run
-// from the ring.  Runs reaching beyond the window and the run that wraps
-// around the table end are read from global memory, which stays intact until
-// the zeroing.
+// clz/ffs in its own 32-slot word and the neighbouring ones, and it ranks its
+// key by reading the run from the ring.  Runs reaching further (rare at the
+// tables' load) and the run that wraps around the table end are read from
+// global memory, which stays intact until the zeroing.  (Searching the whole
+// 384-slot window instead cost 5 % more post-processing time on GB300.)
 constexpr int32_t kBlk4 = 128;
 constexpr int32_t kRing = 4 * kBlk4;
 
@@ -246,23 +247,15 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
                     pos = end - cyc + rank;
                 } else {
                     // the empty window positions before (s) and after (e) the run
+                    // this word and its neighbours only (runs longer than 32
+                    // slots take the global path below)
                     int32_t s = -1, e = 3 * kBlk4;
                     uint32_t z = ~w[4 + j] & lt;
-                    if (z) {
-                        s = 32 * (4 + j) + 31 - __clz(z);
-                    } else {
-#pragma unroll
-                        for (int i = 3 + j; i >= 0; --i)
-                            if (~w[i]) { s = 32 * i + 31 - __clz(~w[i]); break; }
-                    }
+                    if (z) s = 32 * (4 + j) + 31 - __clz(z);
+                    else if (~w[3 + j]) s = 32 * (3 + j) + 31 - __clz(~w[3 + j]);
                     z = ~w[4 + j] & gt;
-                    if (z) {
-                        e = 32 * (4 + j) + __ffs(z) - 1;
-                    } else {
-#pragma unroll
-                        for (int i = 5 + j; i < 12; ++i)
-                            if (~w[i]) { e = 32 * i + __ffs(~w[i]) - 1; break; }
-                    }
+                    if (z) e = 32 * (4 + j) + __ffs(z) - 1;
+                    else if (~w[5 + j]) e = 32 * (5 + j) + __ffs(~w[5 + j]) - 1;
                     uint32_t rank = 0, back;
                     if (s >= 0 && e < 3 * kBlk4) {
                         back = (uint32_t)(p - s - 1);
