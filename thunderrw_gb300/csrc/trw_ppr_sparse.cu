@@ -139,13 +139,15 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 //         among the run's keys)
 // A warp takes 128 slots of its segment per iteration (segments are
 // multiples of 128 slots: tables have at least 2^10 slots, chunks 2^16 at
-// most, 8 warps a CTA), lane l owning slots l, l + 32, l + 64 and l + 96.
-// Keys arrive with 16-byte loads into a per-warp ring of four 128-slot blocks
-// in shared memory (the previous, current and next block, and the one after
-// being filled); four ballots per block give its 128-bit occupancy, from
-// which every slot finds the empty slots before and after its run with
-// clz/ffs in its own 32-slot word and the neighbouring ones, and it ranks its
-// key by reading the run from the ring.  Runs reaching further (rare at the
+// most, 8 warps a CTA).  Keys arrive with 16-byte loads into a per-warp ring
+// of four 128-slot blocks in shared memory (the previous, current and next
+// block, and the one after being filled); four ballots per block give its
+// 128-bit occupancy.  The block's occupied slots are dealt out to the lanes
+// in order (lane l takes occupied slots l, l + 32, ..., located with
+// find-nth-set-bit in the occupancy words), so every lane has a slot to emit
+// instead of 58 % of them idling on empty ones.  Each slot finds the empty
+// slots before and after its run with clz/ffs in its own 32-slot word and the
+// neighbouring ones, and ranks its key by reading the run from the ring.  Runs reaching further (rare at the
 // tables' load) and the run that wraps around the table end are read from
 // global memory, which stays intact until the zeroing.  (Searching the whole
 // 384-slot window instead cost 5 % more post-processing time on GB300.)
@@ -157,6 +159,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
                                                              int64_t capacity, int *error) {
     __shared__ uint32_t wrap[2];
     __shared__ __align__(16) int32_t ring_all[kEmitWarps][kRing];
+    __shared__ uint32_t wsm_all[kEmitWarps][6];  // occupancy words 3 .. 8 of the window
     const uint32_t S = chunks_for(bits);
     const int64_t q = blockIdx.x / S;
     const uint32_t chunk = blockIdx.x % S;
@@ -199,17 +202,11 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
 #pragma unroll
         for (int j = 0; j < 4; ++j) o[j] = __ballot_sync(0xffffffffu, r[32 * j + lane] != 0);
     };
-    auto load_cnts = [&](int32_t m, int32_t(&c)[4]) {
-        const uint32_t y0 = lo + (uint32_t)m * kBlk4 + lane;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) c[j] = m < nblk ? __ldg(cnts + y0 + 32 * j) : 0;
-    };
     reinterpret_cast<int4 *>(ring_of(-1))[lane] = load_blk(-1);
     reinterpret_cast<int4 *>(ring_of(0))[lane] = load_blk(0);
     reinterpret_cast<int4 *>(ring_of(1))[lane] = load_blk(1);
     int4 kf = load_blk(2);
-    int32_t cc[4], cn[4];
-    load_cnts(0, cc);
+    uint32_t *wsm = wsm_all[warp];
     __syncwarp();
     uint32_t w[12];  // occupancy of the window: blocks b - 1, b, b + 1, 32 slots a word
     {
@@ -224,71 +221,86 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
 #pragma unroll
         for (int j = 0; j < 4; ++j) w[8 + j] = o[j];
     }
-    const unsigned lt = lanemask_lt(), gt = ~(lt | (1u << lane));
     for (int32_t b = 0; b < nblk; ++b) {
         reinterpret_cast<int4 *>(ring_of(b + 2))[lane] = kf;  // over block b - 2, read before the last __syncwarp
         kf = load_blk(b + 3);
-        load_cnts(b + 1, cn);
-        const int32_t *rc = ring_of(b);  // window position i (block b - 1 + i / 128) is ring[(b * 128 + i) mod 512]
-        int64_t before = prefix;
+        if (lane == 0) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int32_t k = rc[32 * j + lane];
-            const int32_t p = kBlk4 + 32 * j + lane;  // this slot's window position
-            const uint32_t xs = lo + (uint32_t)b * kBlk4 + 32 * j + lane;
-            if (write && k != 0) {
-                int64_t pos;
-                if (cyc && (xs < head || xs + tail >= nslots)) {  // the wrap-around run: last, keys sorted
-                    uint32_t rank = 0;
-                    for (uint32_t i = 0; i < cyc; ++i) {
-                        const uint32_t y = i < tail ? nslots - tail + i : i - tail;
-                        rank += __ldg(keys + y) < k;
-                    }
-                    pos = end - cyc + rank;
-                } else {
-                    // the empty window positions before (s) and after (e) the run
-                    // this word and its neighbours only (runs longer than 32
-                    // slots take the global path below)
-                    int32_t s = -1, e = 3 * kBlk4;
-                    uint32_t z = ~w[4 + j] & lt;
-                    if (z) s = 32 * (4 + j) + 31 - __clz(z);
-                    else if (~w[3 + j]) s = 32 * (3 + j) + 31 - __clz(~w[3 + j]);
-                    z = ~w[4 + j] & gt;
-                    if (z) e = 32 * (4 + j) + __ffs(z) - 1;
-                    else if (~w[5 + j]) e = 32 * (5 + j) + __ffs(~w[5 + j]) - 1;
-                    uint32_t rank = 0, back;
-                    if (s >= 0 && e < 3 * kBlk4) {
-                        back = (uint32_t)(p - s - 1);
-                        for (int32_t i = s + 1; i < e; ++i)
-                            rank += ring[(b * kBlk4 + i) & (kRing - 1)] < k;  // k itself does not count
-                    } else {  // the run reaches beyond the window
-                        back = 0;
-                        while (xs > back && __ldg(keys + xs - back - 1) != 0) ++back;
-                        for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + xs - d) < k;
-                        for (uint32_t y = xs + 1; y < nslots; ++y) {
-                            const int32_t v = __ldg(keys + y);
-                            if (v == 0) break;
-                            rank += v < k;
-                        }
-                    }
-                    pos = before + __popc(w[4 + j] & lt) - head - back + rank;
-                }
-                vout[pos] = k - 1;
-                cout[pos] = cc[j] + 1;  // the table counts visits after the first
-            }
-            before += __popc(w[4 + j]);
+            for (int i = 0; i < 6; ++i) wsm[i] = w[3 + i];
         }
-        prefix = before;
+        __syncwarp();
+        // the block's occupied slots, compacted: lane l takes occupied slots
+        // l, l + 32, ... of the block (m counts the occupied slots before it)
+        const uint32_t c1 = __popc(w[4]), c2 = c1 + __popc(w[5]), c3 = c2 + __popc(w[6]), n = c3 + __popc(w[7]);
+        for (uint32_t m0 = 0; m0 < n; m0 += 32) {
+            const uint32_t m = m0 + lane;
+            if (!write || m >= n) continue;
+            int wi;
+            uint32_t rem;
+            if (m < c1) { wi = 0; rem = m; }
+            else if (m < c2) { wi = 1; rem = m - c1; }
+            else if (m < c3) { wi = 2; rem = m - c2; }
+            else { wi = 3; rem = m - c3; }
+            const uint32_t wc = wsm[wi + 1];
+            const int bit = (int)__fns(wc, 0, (int)rem + 1);
+            const int32_t p = kBlk4 + 32 * wi + bit;  // this slot's window position
+            const uint32_t xs = lo + (uint32_t)b * kBlk4 + 32 * wi + bit;
+            const int32_t k = ring[(b * kBlk4 + p) & (kRing - 1)];
+            int64_t pos;
+            if (cyc && (xs < head || xs + tail >= nslots)) {  // the wrap-around run: last, keys sorted
+                uint32_t rank = 0;
+                for (uint32_t i = 0; i < cyc; ++i) {
+                    const uint32_t y = i < tail ? nslots - tail + i : i - tail;
+                    rank += __ldg(keys + y) < k;
+                }
+                pos = end - cyc + rank;
+            } else {
+                // the empty window positions before (s) and after (e) the run,
+                // from this word and its neighbours (runs reaching further take
+                // the global path below)
+                int32_t s = -1, e = 3 * kBlk4;
+                uint32_t z = ~wc & ((1u << bit) - 1u);
+                if (z) {
+                    s = 32 * (4 + wi) + 31 - __clz(z);
+                } else {
+                    const uint32_t wp = wsm[wi];
+                    if (~wp) s = 32 * (3 + wi) + 31 - __clz(~wp);
+                }
+                z = ~wc & ~((2u << bit) - 1u);
+                if (z) {
+                    e = 32 * (4 + wi) + __ffs(z) - 1;
+                } else {
+                    const uint32_t wn = wsm[wi + 2];
+                    if (~wn) e = 32 * (5 + wi) + __ffs(~wn) - 1;
+                }
+                uint32_t rank = 0, back;
+                if (s >= 0 && e < 3 * kBlk4) {
+                    back = (uint32_t)(p - s - 1);
+                    for (int32_t i = s + 1; i < e; ++i)
+                        rank += ring[(b * kBlk4 + i) & (kRing - 1)] < k;  // k itself does not count
+                } else {  // the run reaches beyond the window
+                    back = 0;
+                    while (xs > back && __ldg(keys + xs - back - 1) != 0) ++back;
+                    for (uint32_t d = 1; d <= back; ++d) rank += __ldg(keys + xs - d) < k;
+                    for (uint32_t y = xs + 1; y < nslots; ++y) {
+                        const int32_t v = __ldg(keys + y);
+                        if (v == 0) break;
+                        rank += v < k;
+                    }
+                }
+                pos = prefix + m - head - back + rank;
+            }
+            vout[pos] = k - 1;
+            cout[pos] = __ldg(cnts + xs) + 1;  // the table counts visits after the first
+        }
+        prefix += n;
         __syncwarp();
         uint32_t o[4];
         ballots(b + 2, o);
 #pragma unroll
         for (int j = 0; j < 8; ++j) w[j] = w[j + 4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            w[8 + j] = o[j];
-            cc[j] = cn[j];
-        }
+        for (int j = 0; j < 4; ++j) w[8 + j] = o[j];
     }
     if (S > 1) return;  // chunked tables are zeroed after the kernel: other CTAs may still read this chunk
     __syncthreads();
