@@ -139,7 +139,8 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 //         among the run's keys)
 // A warp takes 128 slots of its segment per iteration (segments are
 // multiples of 128 slots: tables have at least 2^10 slots, chunks 2^16 at
-// most, 8 warps a CTA).  Keys arrive with 16-byte loads into a per-warp ring
+// most, 8 warps a CTA).  Counts arrive two blocks ahead into a per-warp
+// buffer of the current block.  Keys arrive with 16-byte loads into a per-warp ring
 // of four 128-slot blocks in shared memory (the previous, current and next
 // block, and the one after being filled); four ballots per block give its
 // 128-bit occupancy.  The block's occupied slots are dealt out to the lanes
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     __shared__ uint32_t wrap[2];
     __shared__ __align__(16) int32_t ring_all[kEmitWarps][kRing];
     __shared__ uint32_t wsm_all[kEmitWarps][6];  // occupancy words 3 .. 8 of the window
+    __shared__ __align__(16) int32_t cnt_all[kEmitWarps][kBlk4];  // counts of the current block
     const uint32_t S = chunks_for(bits);
     const int64_t q = blockIdx.x / S;
     const uint32_t chunk = blockIdx.x % S;
@@ -206,6 +208,14 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     reinterpret_cast<int4 *>(ring_of(0))[lane] = load_blk(0);
     reinterpret_cast<int4 *>(ring_of(1))[lane] = load_blk(1);
     int4 kf = load_blk(2);
+    // counts of block m (16 bytes a lane), loaded two blocks ahead so that no
+    // iteration waits on a DRAM round trip for them
+    const int4 *c4 = reinterpret_cast<const int4 *>(cnts);
+    auto load_cnt = [&](int32_t m) {
+        return m < nblk ? __ldg(c4 + (((int64_t)lo + (int64_t)m * kBlk4) >> 2) + lane) : make_int4(0, 0, 0, 0);
+    };
+    int4 ca = load_cnt(0), cb = load_cnt(1);
+    int32_t *cbuf = cnt_all[warp];
     uint32_t *wsm = wsm_all[warp];
     __syncwarp();
     uint32_t w[12];  // occupancy of the window: blocks b - 1, b, b + 1, 32 slots a word
@@ -224,6 +234,9 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
     for (int32_t b = 0; b < nblk; ++b) {
         reinterpret_cast<int4 *>(ring_of(b + 2))[lane] = kf;  // over block b - 2, read before the last __syncwarp
         kf = load_blk(b + 3);
+        reinterpret_cast<int4 *>(cbuf)[lane] = ca;  // over block b - 1's, read before the last __syncwarp
+        ca = cb;
+        cb = load_cnt(b + 2);
         if (lane == 0) {
 #pragma unroll
             for (int i = 0; i < 6; ++i) wsm[i] = w[3 + i];
@@ -291,7 +304,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int
                 pos = prefix + m - head - back + rank;
             }
             vout[pos] = k - 1;
-            cout[pos] = __ldg(cnts + xs) + 1;  // the table counts visits after the first
+            cout[pos] = cbuf[32 * wi + bit] + 1;  // the table counts visits after the first
         }
         prefix += n;
         __syncwarp();
