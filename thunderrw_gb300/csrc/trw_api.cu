@@ -81,6 +81,9 @@ constexpr int kMaxRanges = 16;  // walker ranges of a host-output walk (the pipe
 // fewer than 16 units of 8 walkers per lane use at most kPprRanges equal
 // ranges.
 constexpr int kPprRanges = 8;
+// Post-processing chunks of a host-output batch: 2^14 slots a CTA (2^16 for
+// device outputs, where the whole batch fills the GPU with tables).
+constexpr int32_t kPprRangeChunkBits = 14;
 constexpr int kPprSplit[] = {1, 1, 2, 2, 2, 2, 2, 2, 1, 1};
 constexpr int kPprSplitUnits = 16;  // sum of kPprSplit
 
@@ -1106,13 +1109,6 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
         g->ppr_bits = bits;
         g->ppr_queries = num_queries;
     }
-    const int64_t dist_ints = ppr_distinct_ints(bits);  // per query: total + segment prefixes
-    const size_t b_dist = align_up(sizeof(int32_t) * (size_t)dist_ints * (size_t)std::max<int64_t>(1, num_queries));
-    TRW_CUDA(g->ppr_distinct.ensure(b_dist + sizeof(uint64_t) * (kMaxRanges + 1)));
-    int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
-    int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
-    uint64_t *d_steps = reinterpret_cast<uint64_t *>(static_cast<char *>(g->ppr_distinct.p) + b_dist);
-
     // staging for host buffers: sources in; offsets, vertices, counts out
     const bool h_src = num_queries > 0 && !is_device_ptr(sources);
     const bool h_off = !is_device_ptr(offsets);
@@ -1120,6 +1116,17 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
     const bool h_c = counts && !is_device_ptr(counts);
     const bool h_steps = steps && !is_device_ptr(steps);
     const bool host_out = h_off || h_v || h_c;
+    // With host outputs the batch runs as ranges of queries (below), each
+    // post-processed while the next range walks; smaller post-processing
+    // chunks keep one range's emit from running as a single long wave.
+    const int32_t cbits = host_out ? kPprRangeChunkBits : kPprChunkBits;
+    const int64_t dist_ints = ppr_distinct_ints(bits, cbits);  // per query: total + segment prefixes
+    const size_t b_dist = align_up(sizeof(int32_t) * (size_t)dist_ints * (size_t)std::max<int64_t>(1, num_queries));
+    TRW_CUDA(g->ppr_distinct.ensure(b_dist + sizeof(uint64_t) * (kMaxRanges + 1)));
+    int32_t *tables = static_cast<int32_t *>(g->ppr_tables.p);
+    int32_t *distinct = static_cast<int32_t *>(g->ppr_distinct.p);
+    uint64_t *d_steps = reinterpret_cast<uint64_t *>(static_cast<char *>(g->ppr_distinct.p) + b_dist);
+
     const size_t b_src = h_src ? align_up(sizeof(int32_t) * (size_t)num_queries) : 0;
     if (h_src) TRW_CUDA(g->stage.ensure(b_src));
     const size_t b_off = h_off ? align_up(sizeof(int64_t) * (size_t)(num_queries + 1)) : 0;
@@ -1197,9 +1204,9 @@ int trw_ppr_batch_sparse(trw_graph *g, const trw_walk_desc *desc, const int32_t 
             return rc;
         }
         if (nr > 0 && rs[1] != st) TRW_CUDA(cudaStreamWaitEvent(sr, g->offsets_done[nr - 1], 0));
-        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, sr));
+        TRW_CUDA(launch_ppr_offsets(tab, bits, dist, nq, d_off + qs, sr, cbits));
         if (host_out) TRW_CUDA(cudaEventRecord(g->offsets_done[nr], sr));
-        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, sr));
+        TRW_CUDA(launch_ppr_emit(tab, bits, nq, d_off + qs, dist, d_v, d_c, capacity, g->error, sr, cbits));
         if (host_out) {
             TRW_CUDA(cudaMemcpyAsync(g->h_ends + nr, d_off + qs + nq, sizeof(int64_t), cudaMemcpyDeviceToHost, sr));
             TRW_CUDA(cudaEventRecord(g->range_done[nr], sr));

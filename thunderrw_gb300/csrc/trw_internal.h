@@ -52,15 +52,21 @@ struct MultiBatch {
 cudaError_t launch_walk_multi(const MultiBatch &mb, int64_t total_walkers, int64_t total_chunks, int sampler,
                               int update, int weight_kind, int num_sms, cudaStream_t st);
 
+// Sparse PPR post-processing takes a table in chunks of at most
+// 2^chunk_bits slots, one CTA each (10 <= chunk_bits <= 16); the same
+// chunk_bits must reach ppr_distinct_ints, launch_ppr_offsets and
+// launch_ppr_emit of one batch.  A chunked table (more than one chunk) is
+// zeroed by a memset after its emit instead of by the emit's CTA.
+constexpr int32_t kPprChunkBits = 16;
 // offsets[0] must hold the entries before this range of queries (0 for the first)
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
-                               cudaStream_t st);
+                               cudaStream_t st, int32_t chunk_bits = kPprChunkBits);
 // `distinct` holds nq totals followed by ppr_distinct_ints(bits) - 1 segment
 // prefixes per query (ppr_distinct_ints(bits) ints per query in all)
-int64_t ppr_distinct_ints(int32_t bits);
+int64_t ppr_distinct_ints(int32_t bits, int32_t chunk_bits = kPprChunkBits);
 cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
                             const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
-                            cudaStream_t st);
+                            cudaStream_t st, int32_t chunk_bits = kPprChunkBits);
 // *out = parts[0] + ... + parts[n-1], on the device
 cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaStream_t st);
 

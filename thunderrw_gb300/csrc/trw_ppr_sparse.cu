@@ -59,20 +59,21 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T *warp_sums, T &total) {
 }
 
 constexpr int kEmitWarps = kEmitThreads / 32;  // table segments per CTA
-constexpr int32_t kChunkBits = 16;             // at most 2^16 slots per CTA
 
-// A table of 2^bits slots is split into chunks_for(bits) chunks of at most
-// 2^16 slots, one CTA each, and every chunk into kEmitWarps warp segments;
-// a single large table (a query with many walkers) is then spread over the
-// GPU instead of one CTA.
-__host__ __device__ inline uint32_t chunks_for(int32_t bits) {
-    return bits > kChunkBits ? 1u << (bits - kChunkBits) : 1u;
+// A table of 2^bits slots is split into chunks_for(bits, cbits) chunks of at
+// most 2^cbits slots (2^16 by default), one CTA each, and every chunk into
+// kEmitWarps warp segments; a single large table (a query with many walkers)
+// is then spread over the GPU instead of one CTA.  Smaller chunks shorten a
+// CTA's run where few tables fill the GPU (the ranges of a host-output batch).
+__host__ __device__ inline uint32_t chunks_for(int32_t bits, int32_t cbits) {
+    return bits > cbits ? 1u << (bits - cbits) : 1u;
 }
 
 // Occupied slots (distinct visited vertices) per warp segment: seg[(q * S +
 // chunk) * kEmitWarps + warp].
-__global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *tables, int32_t bits, int32_t *seg) {
-    const uint32_t S = chunks_for(bits);
+__global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *tables, int32_t bits, int32_t cbits,
+                                                                 int32_t *seg) {
+    const uint32_t S = chunks_for(bits, cbits);
     const int64_t q = blockIdx.x / S;
     const uint32_t c = blockIdx.x % S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -91,10 +92,11 @@ __global__ void __launch_bounds__(kEmitThreads) distinct_kernel(const int32_t *t
 
 // Per query: the segment counts become their exclusive prefix within the
 // query (in place) and the query's total goes to distinct[q].
-__global__ void __launch_bounds__(kScanThreads) segment_scan_kernel(int32_t *seg, int32_t bits, int32_t *distinct) {
+__global__ void __launch_bounds__(kScanThreads) segment_scan_kernel(int32_t *seg, int32_t bits, int32_t cbits,
+                                                                     int32_t *distinct) {
     __shared__ int32_t sums[32];
     const int64_t q = blockIdx.x;
-    const int32_t n = (int32_t)chunks_for(bits) * kEmitWarps;
+    const int32_t n = (int32_t)chunks_for(bits, cbits) * kEmitWarps;
     int32_t *v = seg + q * n;
     int32_t carry = 0;
     for (int32_t b = 0; b < n; b += kScanThreads) {
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
     if (threadIdx.x == 0) offsets[nq] = carry;
 }
 
-// One CTA per chunk of at most 2^16 slots of a query's table, one contiguous
+// One CTA per chunk of at most 2^cbits slots of a query's table, one contiguous
 // segment of the chunk per warp.
 //
 // Output order.  Inserts probe linearly and wrap from the last slot to slot
@@ -138,8 +140,8 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 //         start) - (its distance back to the run start) + (rank of its key
 //         among the run's keys)
 // A warp takes 128 slots of its segment per iteration (segments are
-// multiples of 128 slots: tables have at least 2^10 slots, chunks 2^16 at
-// most, 8 warps a CTA).  Counts arrive two blocks ahead into a per-warp
+// multiples of 128 slots: tables have at least 2^10 slots, chunks 2^10 to
+// 2^16, 8 warps a CTA).  Counts arrive two blocks ahead into a per-warp
 // buffer of the current block.  Keys arrive with 16-byte loads into a per-warp ring
 // of four 128-slot blocks in shared memory (the previous, current and next
 // block, and the one after being filled); four ballots per block give its
@@ -155,14 +157,15 @@ __global__ void __launch_bounds__(kScanThreads) offsets_kernel(const int32_t *di
 constexpr int32_t kBlk4 = 128;
 constexpr int32_t kRing = 4 * kBlk4;
 
-__global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, const int64_t *offsets,
-                                                             const int32_t *seg_prefix, int32_t *vout, int32_t *cout,
-                                                             int64_t capacity, int *error) {
+__global__ void __launch_bounds__(kEmitThreads) emit_kernel(int32_t *tables, int32_t bits, int32_t cbits,
+                                                             const int64_t *offsets, const int32_t *seg_prefix,
+                                                             int32_t *vout, int32_t *cout, int64_t capacity,
+                                                             int *error) {
     __shared__ uint32_t wrap[2];
     __shared__ __align__(16) int32_t ring_all[kEmitWarps][kRing];
     __shared__ uint32_t wsm_all[kEmitWarps][6];  // occupancy words 3 .. 8 of the window
     __shared__ __align__(16) int32_t cnt_all[kEmitWarps][kBlk4];  // counts of the current block
-    const uint32_t S = chunks_for(bits);
+    const uint32_t S = chunks_for(bits, cbits);
     const int64_t q = blockIdx.x / S;
     const uint32_t chunk = blockIdx.x % S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -335,14 +338,16 @@ cudaError_t launch_sum_steps(const uint64_t *parts, int n, uint64_t *out, cudaSt
     return cudaGetLastError();
 }
 
-int64_t ppr_distinct_ints(int32_t bits) { return 1 + (int64_t)chunks_for(bits) * kEmitWarps; }
+int64_t ppr_distinct_ints(int32_t bits, int32_t chunk_bits) {
+    return 1 + (int64_t)chunks_for(bits, chunk_bits) * kEmitWarps;
+}
 
 cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *distinct, int64_t nq, int64_t *offsets,
-                               cudaStream_t st) {
+                               cudaStream_t st, int32_t chunk_bits) {
     if (nq > 0) {
-        const int64_t ctas = nq * chunks_for(bits);
-        distinct_kernel<<<(unsigned)ctas, kEmitThreads, 0, st>>>(tables, bits, distinct + nq);
-        segment_scan_kernel<<<(unsigned)nq, kScanThreads, 0, st>>>(distinct + nq, bits, distinct);
+        const int64_t ctas = nq * chunks_for(bits, chunk_bits);
+        distinct_kernel<<<(unsigned)ctas, kEmitThreads, 0, st>>>(tables, bits, chunk_bits, distinct + nq);
+        segment_scan_kernel<<<(unsigned)nq, kScanThreads, 0, st>>>(distinct + nq, bits, chunk_bits, distinct);
     }
     offsets_kernel<<<1, kScanThreads, 0, st>>>(distinct, nq, offsets);
     return cudaGetLastError();
@@ -350,11 +355,11 @@ cudaError_t launch_ppr_offsets(const int32_t *tables, int32_t bits, int32_t *dis
 
 cudaError_t launch_ppr_emit(int32_t *tables, int32_t bits, int64_t nq, const int64_t *offsets,
                             const int32_t *distinct, int32_t *vout, int32_t *cout, int64_t capacity, int *error,
-                            cudaStream_t st) {
+                            cudaStream_t st, int32_t chunk_bits) {
     if (nq <= 0) return cudaSuccess;
-    const uint32_t S = chunks_for(bits);
-    emit_kernel<<<(unsigned)(nq * S), kEmitThreads, 0, st>>>(tables, bits, offsets, distinct + nq, vout, cout,
-                                                             capacity, error);
+    const uint32_t S = chunks_for(bits, chunk_bits);
+    emit_kernel<<<(unsigned)(nq * S), kEmitThreads, 0, st>>>(tables, bits, chunk_bits, offsets, distinct + nq, vout,
+                                                             cout, capacity, error);
     if (S > 1) return cudaMemsetAsync(tables, 0, sizeof(int32_t) * 2 * ((size_t)nq << bits), st);
     return cudaGetLastError();
 }
